@@ -1,0 +1,393 @@
+#!/usr/bin/env python3
+"""Benchmark of the D2Q9 pull stream-collide hot path on GB300.
+
+Workload (the reference's at-scale channel workload at the size its HBM target is quoted on):
+walled channel 4096 x 4096, periodic in x, tau 0.6, body force (1e-6, 0), populations
+f_i - w_i initialised from the seeded SplitMix64 perturbation in [-1e-4, 1e-4], plain FP32
+(bit-exact with the reference's v0). One bench step = one lattice time step over the whole grid
+(one launch of the fused step kernel). MLUPS = nx * ny * steps / time / 1e6, solid cells
+included (reference src/common/driver.hpp:120).
+
+  value     device-resident state, K steps timed with CUDA events on the solver's stream,
+            barrier + synchronize on both sides, max over ranks.
+  e2e       the same metric through the public C ABI with host buffers: each e2e step is one
+            user job, upload of the initial state from pinned host memory (9 N floats), 1000
+            lattice steps, download of rho/ux/uy (3 N floats), all inside the timed region.
+  roofline  HBM-bound: algorithmic bytes per cell update 2 * 9 * sizeof(float) = 72 B; achieved
+            = 72 B * N / (average step-kernel duration); peak = measured copy bandwidth
+            (MEASURED_PEAKS.json hbm_gbs); traffic = ncu DRAM bytes per launch (profiles/).
+  forms     the other forms on the same grid: FP64 (144 B/cell), FP16 and BF16 storage (36 B).
+  cpu_baseline  the oracle's OpenMP port of the reference's v1 solver on the host cores.
+
+--impl reference: the reference's CPU implementation of the path (the oracle's port of v1,
+bitwise identical to v0; the reference's own sources are not present on the GPU host) on all
+host cores, same metric and workload, rank 0 only.
+
+Inputs are larger than L2 (604 MB per population buffer vs 129 MB), so no L2 flush is needed.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "MLUPS & % of 72B/cell HBM roofline, 1 GB300: plain vs fp16-store vs adjoint"
+SEED, AMP = 20240917, 1e-4
+TAU, FX, FY = 0.6, 1e-6, 0.0
+BYTES_PER_CELL = {"fp32": 72, "fp64": 144, "fp16": 36, "bf16": 36}
+HBM_FALLBACK_GBS = 6800.0
+E2E_LATTICE_STEPS = 1000
+
+
+def measured_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return HBM_FALLBACK_GBS, "fallback"
+
+
+def profiled_traffic(precision: str, n: int):
+    """DRAM bytes per step launch from the committed ncu summary, scaled to this grid."""
+    f = ROOT / "profiles" / f"pull_step_{precision}_traffic.txt"
+    if not f.exists():
+        return None
+    vals = {}
+    for line in f.read_text().splitlines():
+        if ":" in line and not line.startswith("#"):
+            k, v = line.split(":", 1)
+            vals[k.strip()] = v.strip()
+    try:
+        per_cell = float(vals["dram_bytes_per_cell"])
+    except (KeyError, ValueError):
+        return None
+    return per_cell * n * n
+
+
+class ClockSampler:
+    """nvidia-smi SM clock and throttle-reason samples during the timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self._stop = threading.Event()
+        self._t = None
+        self.window = (0.0, 0.0)
+
+    def start(self):
+        self._t = threading.Thread(target=self._loop, daemon=True)
+        self._t.start()
+
+    def _loop(self):
+        while not self._stop.is_set():
+            try:
+                out = subprocess.run(
+                    ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                     "--format=csv,noheader,nounits"], capture_output=True, text=True, timeout=5)
+                row = [c.strip() for c in out.stdout.strip().split(",")]
+                if len(row) >= 8:
+                    self.samples.append((time.time(), row))
+            except Exception:
+                pass
+            self._stop.wait(0.1)
+
+    def stop(self):
+        self._stop.set()
+        if self._t:
+            self._t.join(timeout=10)
+
+    def summary(self):
+        t0, t1 = self.window
+        inside = [r for t, r in self.samples if t0 <= t <= t1]
+        if not inside and self.samples:  # very short timed region: nearest samples
+            mid = 0.5 * (t0 + t1)
+            inside = [min(self.samples, key=lambda s: abs(s[0] - mid))[1]]
+        if not inside:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[0]) for r in inside if num(r[0]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in inside for k in range(4) if "Active" in r[4 + k]})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": num(inside[0][1]), "reasons": reasons, "samples": len(inside),
+                "power_w_median": statistics.median([num(r[2]) for r in inside if num(r[2])] or [0])}
+
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl"
+        dist.init_process_group(backend=backend)
+    return rank, local, world, dist
+
+
+def barrier(dist):
+    if dist is not None:
+        dist.barrier()
+
+
+def max_over_ranks(x: float, dist) -> float:
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def channel_state(orc, n: int, precision_real: str):
+    import __graft_entry__ as entry
+    pkg = entry.package()
+    mask = pkg.make_channel(n, n)
+    s0 = orc.seeded_state(SEED, AMP, n, n, mask, precision_real)
+    return pkg, mask, s0
+
+
+def time_form(pkg, mask, s0, n, precision, steps, warmup):
+    """Device-resident MLUPS of one form (CUDA events on the solver's stream)."""
+    with pkg.Solver(n, n, TAU, FX, FY, mask, precision=precision) as s:
+        s.set_populations(s0)
+        s.run(warmup)
+        t = s.timed_run(steps)
+    return n * n * steps / t / 1e6, t
+
+
+def cpu_baseline(orc, n: int, budget_s: float = 8.0):
+    """Oracle port of the reference's v1 solver (OpenMP, all host threads), bounded sample."""
+    threads = os.cpu_count() or 1
+    rows = n
+    mask = np.zeros(n * rows, np.uint8)
+    mask[:n] = 1
+    mask[-n:] = 1
+    s0 = orc.seeded_state(SEED, AMP, n, rows, mask, "f32")
+    r = orc.s_to_r(n, rows, mask, s0, real="f32")
+    del s0
+    t0 = time.perf_counter()
+    orc.pull_run(n, rows, mask, TAU, FX, FY, r, 1, real="f32", threads=threads)
+    one = time.perf_counter() - t0
+    steps = int(max(1, min(50, budget_s / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    orc.pull_run(n, rows, mask, TAU, FX, FY, r, steps, real="f32", threads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": n * rows * steps / dt / 1e6, "unit": "MLUPS", "cores": threads,
+            "kind": "port",
+            "sample": f"{n}x{rows} walled channel, {steps} steps after 1 warm-up step, FP32, "
+                      f"oracle pull port of reference v1 (src/v1_omp/solver_v1.cpp), "
+                      f"{threads} OpenMP threads"}
+
+
+def run_ours(args):
+    import torch
+
+    import __graft_entry__ as entry
+    rank, local, world, dist = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    pkg = entry.package()
+    pkg.build()
+    orc = entry.oracle_module()
+    if not orc.LIB.exists():
+        orc.build()
+    n = args.nx
+    warmup = max(args.warmup, 3)
+    _, mask, s0 = channel_state(orc, n, "f32")
+
+    solver = pkg.Solver(n, n, TAU, FX, FY, mask, precision="fp32")
+    solver.set_populations(s0)
+    solver.run(warmup)
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier(dist)
+    torch.cuda.synchronize()
+    solver.synchronize()
+    t_start = time.time()
+    secs = solver.timed_run(args.steps)
+    torch.cuda.synchronize()
+    barrier(dist)
+    sampler.window = (t_start, time.time())
+    time.sleep(0.25)
+    sampler.stop()
+    secs = max_over_ranks(secs, dist)
+    info = solver.bench_info()
+    solver.close()
+
+    cells = n * n
+    value = cells * args.steps * world / secs / 1e6
+    step_s = secs / args.steps
+    peak, peak_kind = measured_peak()
+    achieved = BYTES_PER_CELL["fp32"] * cells / step_s / 1e9
+    traffic = profiled_traffic("fp32", n)
+
+    # e2e through the public API: pinned host input, 1000 steps, host output.
+    e2e = None
+    if args.e2e_jobs > 0:
+        pin = torch.empty(s0.size, dtype=torch.float32).pin_memory()
+        pin.numpy()[:] = s0
+        outs = [torch.empty(cells, dtype=torch.float32).pin_memory() for _ in range(3)]
+        with pkg.Solver(n, n, TAU, FX, FY, mask, precision="fp32") as s:
+            s.set_populations(pin.numpy())
+            s.run(10)
+            s.macroscopic([o.numpy() for o in outs])
+            barrier(dist)
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            for _ in range(args.e2e_jobs):
+                s.set_populations(pin.numpy())
+                s.run(E2E_LATTICE_STEPS)
+                s.macroscopic([o.numpy() for o in outs])
+            torch.cuda.synchronize()
+            barrier(dist)
+            dt = max_over_ranks(time.perf_counter() - t0, dist)
+        e2e = {"value": cells * E2E_LATTICE_STEPS * args.e2e_jobs * world / dt / 1e6,
+               "unit": "MLUPS", "h2d_bytes_per_step": int(s0.nbytes),
+               "d2h_bytes_per_step": int(3 * cells * 4),
+               "lattice_steps_per_e2e_step": E2E_LATTICE_STEPS, "e2e_steps": args.e2e_jobs,
+               "api": "lbm_set_populations + lbm_run(1000) + lbm_macroscopic (C ABI)"}
+
+    forms = {}
+    if args.forms and rank == 0:
+        for prec, steps in (("fp16", 400), ("bf16", 400), ("fp64", 100)):
+            try:
+                st = s0.astype(np.float64) if prec == "fp64" else s0
+                ml, _ = time_form(pkg, mask, st, n, prec, steps, 20)
+                gbs = BYTES_PER_CELL[prec] * ml * 1e6 / 1e9
+                forms[prec] = {"mlups": round(ml, 1), "bytes_per_cell": BYTES_PER_CELL[prec],
+                               "achieved_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
+                               "steps": steps}
+            except Exception as e:  # a form that fails is reported, not hidden
+                forms[prec] = {"error": str(e)[:200]}
+        forms["fp32"] = {"mlups": round(value / world, 1), "bytes_per_cell": 72,
+                         "achieved_gbs": round(achieved, 1), "hbm_frac": round(achieved / peak, 4)}
+        if "mlups" in forms.get("fp16", {}):
+            forms["fp16_over_fp32"] = round(forms["fp16"]["mlups"] / forms["fp32"]["mlups"], 3)
+
+    cpu = None
+    if rank == 0 and args.cpu_baseline:
+        cpu = cpu_baseline(orc, n)
+
+    if rank != 0:
+        return
+    line = {
+        "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world,
+        "steps": args.steps, "warmup": warmup, "ms_per_step": round(step_s * 1e3, 5),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic: seeded SplitMix64 perturbation of f_i - w_i in [-1e-4, 1e-4]",
+        "config": {"workload": f"walled channel {n}x{n}, periodic x, tau 0.6, F=(1e-6,0), "
+                               "plain FP32 pull stream-collide (bit-exact with reference v0)",
+                   "nx": n, "ny": n, "form": "fp32", "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (population buffer 604 MB > 129 MB), no flush"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
+                     "unit": "GB/s", "frac": round(achieved / peak, 4),
+                     "traffic": traffic, "peak_kind": peak_kind,
+                     "algorithmic_bytes_per_launch": BYTES_PER_CELL["fp32"] * cells},
+        "clocks": sampler.summary(),
+        "gpu_launches": args.steps,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+        "forms": forms or None,
+        "device": json.loads("{" + info + "}"),
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_reference(args):
+    """The reference's CPU path (oracle port of v1) on the host cores, rank 0 only."""
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    import __graft_entry__ as entry
+    orc = entry.oracle_module()
+    if not orc.LIB.exists():
+        orc.build()
+    n = args.nx
+    threads = os.cpu_count() or 1
+    warmup = max(args.warmup, 3)
+    # Each bench step is one lattice step; the grid keeps all 4096 columns but its rows are
+    # bounded so that warm-up + timed steps stay within about two minutes.
+    mask_full_row = np.ones(n, np.uint8)
+    rows = n
+    probe_rows = 256
+    pm = np.zeros(n * probe_rows, np.uint8)
+    pm[:n] = 1
+    pm[-n:] = 1
+    pr = orc.s_to_r(n, probe_rows, pm, orc.seeded_state(SEED, AMP, n, probe_rows, pm, "f32"))
+    t0 = time.perf_counter()
+    orc.pull_run(n, probe_rows, pm, TAU, FX, FY, pr, 2, threads=threads)
+    per_cell = (time.perf_counter() - t0) / (2 * n * probe_rows)
+    budget = 120.0
+    while rows > 1024 and per_cell * n * rows * (args.steps + warmup) > budget:
+        rows //= 2
+    mask = np.zeros(n * rows, np.uint8)
+    mask[:n] = mask_full_row
+    mask[-n:] = mask_full_row
+    r = orc.s_to_r(n, rows, mask, orc.seeded_state(SEED, AMP, n, rows, mask, "f32"))
+    orc.pull_run(n, rows, mask, TAU, FX, FY, r, warmup, threads=threads)
+    t0 = time.perf_counter()
+    orc.pull_run(n, rows, mask, TAU, FX, FY, r, args.steps, threads=threads)
+    dt = time.perf_counter() - t0
+    value = n * rows * args.steps / dt / 1e6
+    sample = (f"{n}x{rows} walled channel (full {n}x{n} rows bounded to fit ~2 min), "
+              f"{args.steps} timed lattice steps after {warmup}, FP32, oracle pull port of "
+              f"reference v1 (src/v1_omp/solver_v1.cpp), {threads} OpenMP threads")
+    line = {
+        "impl": "reference", "metric": METRIC, "value": round(value, 2), "unit": "MLUPS",
+        "n_gpus": int(os.environ.get("WORLD_SIZE", "1")), "steps": args.steps, "warmup": warmup,
+        "ms_per_step": round(dt / args.steps * 1e3, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"walled channel {n}x{n}, periodic x, tau 0.6, F=(1e-6,0), "
+                               "plain FP32 pull stream-collide", "nx": n, "ny": rows},
+        "cpu_baseline": {"value": round(value, 2), "unit": "MLUPS", "cores": threads,
+                         "kind": "port", "sample": sample},
+        "e2e": {"value": round(value, 2), "unit": "MLUPS", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser(description=__doc__,
+                                 formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5000)
+    ap.add_argument("--warmup", type=int, default=100)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--nx", type=int, default=4096)
+    ap.add_argument("--e2e-jobs", type=int, default=3)
+    ap.add_argument("--no-forms", dest="forms", action="store_false")
+    ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    args = ap.parse_args()
+    if args.steps < 1:
+        ap.error("--steps must be >= 1")
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,148 @@
+/*
+ * lbm_b200.h - C ABI of the GB300 (sm_103a) D2Q9 lattice-Boltzmann library.
+ *
+ * The library runs the hot path of the reference solver (H-HABCHANE "Simulation de fluide par
+ * la methode de Boltzmann sur reseau", reference paths below are relative to that project):
+ * the fused pull-scheme stream-collide step on structure-of-arrays planes of shifted populations
+ * g_i = f_i - w_i (D2Q9, BGK, Guo body force, halfway bounce-back on a solid mask, periodic in
+ * x and y, optional open inflow/outflow in x) and the rho/u moment pass.
+ *
+ * The reference has no C ABI: its solvers are C++ classes used through templates
+ * (src/common/driver.hpp:5-16). Each entry point below replaces one member of the reference's
+ * GPU solver class lbm::SolverV3 (src/v3_cuda_opt/solver_v3.hpp:27-57); the header-only C++
+ * wrapper lbm_b200.hpp maps them back onto that member set.
+ *
+ * Conventions
+ *   - Every function returns an int status (LBM_OK = 0). No C++ exception crosses this ABI.
+ *     lbm_last_error() describes the last failure of a solver.
+ *   - Host arrays use the reference's v0 layout: populations s[(y*nx + x)*9 + i] (post-streaming,
+ *     shifted), fields f[y*nx + x]. The element type is the solver's host type: float for
+ *     LBM_FP32 / LBM_FP16_STORE / LBM_BF16_STORE, double for LBM_FP64.
+ *   - Direction order 0: rest, 1: +x, 2: +y, 3: -x, 4: -y, 5: (+,+), 6: (-,+), 7: (-,-),
+ *     8: (+,-) (src/common/d2q9.hpp:14-25).
+ *   - All work of a solver is issued on its stream (lbm_set_stream); functions returning host
+ *     data synchronise that stream.
+ */
+#ifndef LBM_B200_H
+#define LBM_B200_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Status codes. */
+enum {
+  LBM_OK = 0,
+  LBM_ERR_INVALID_ARG = 1, /* the reference throws std::invalid_argument (solver_v3.cu:169-170) */
+  LBM_ERR_CUDA = 2,        /* a CUDA runtime error (the reference aborts, cuda_check.hpp:17-27) */
+  LBM_ERR_OUT_OF_MEMORY = 3,
+  LBM_ERR_DIVERGED = 4, /* non-finite density (the reference's driver throws, driver.hpp:217-218) */
+  LBM_ERR_UNSUPPORTED = 5
+};
+
+/* Storage / arithmetic forms. FP32 and FP64 are bit-exact with the reference's v0 in float and
+ * double. FP16_STORE / BF16_STORE keep g_i * scale_i in 16 bits and compute in FP32. */
+typedef enum {
+  LBM_FP32 = 0,
+  LBM_FP64 = 1,
+  LBM_FP16_STORE = 2,
+  LBM_BF16_STORE = 3
+} lbm_precision;
+
+typedef struct lbm_solver lbm_solver;
+
+/* Library version string. */
+const char* lbm_version(void);
+
+/* Replaces SolverV3::SolverV3(nx, ny, tau, fx, fy, Mask) (src/v3_cuda_opt/solver_v3.cu:166-186).
+ * solid: nx*ny bytes, row-major, non-zero = solid. tau, fx, fy are rounded to the solver
+ * precision first (the reference receives them as `real`). Errors: LBM_ERR_INVALID_ARG for
+ * nx < 1, ny < 1, a null mask or tau <= 0.5 (solver_v3.cu:169-170); LBM_ERR_OUT_OF_MEMORY. */
+int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, double fy,
+               int precision, lbm_solver** out);
+
+/* Replaces SolverV3::~SolverV3 (solver_v3.cu:188-192). Null is accepted. */
+int lbm_destroy(lbm_solver* s);
+
+/* Message of the last failed call on s ("" if none). Valid until the next call on s. */
+const char* lbm_last_error(const lbm_solver* s);
+
+/* Uses `stream` (a cudaStream_t, 0 = legacy default stream) for all later work of s. The
+ * reference runs on the legacy default stream (solver_v3.cu:259-264). */
+int lbm_set_stream(lbm_solver* s, void* stream);
+
+/* Replaces SolverV3::set_inflow_outflow(u_in) (solver_v3.cu:228-232): open domain in x, inlet
+ * velocity (u_in, 0) at x = 0, zero-gradient outlet at x = nx - 1. Call before the initial
+ * state is set. Requires nx >= 3. */
+int lbm_set_inflow_outflow(lbm_solver* s, double u_in);
+
+/* Replaces SolverV3::init_equilibrium(rho0, ux0, uy0) (solver_v3.cu:194-226): every fluid cell
+ * at the equilibrium of (rho0, ux0, uy0), solid cells 0. Built on the device. */
+int lbm_init_equilibrium(lbm_solver* s, double rho0, double ux0, double uy0);
+
+/* Sets the post-streaming state from a host array in v0 layout (nx*ny*9 values of the host
+ * type); solid cells are ignored. The reference can only set a state through
+ * init_equilibrium(); this generalises it to any state (converted to the pull state on the
+ * device, by the preimage of streaming). */
+int lbm_set_populations(lbm_solver* s, const void* s_host);
+
+/* Enqueues `steps` time steps (asynchronous). Replaces `steps` calls of SolverV3::step()
+ * (solver_v3.cu:251-278); steps >= 0. */
+int lbm_step(lbm_solver* s, int steps);
+
+/* Replaces SolverV3::run(steps) (solver_v3.cu:280-283): steps, then waits for them. */
+int lbm_run(lbm_solver* s, int steps);
+
+/* Replaces SolverV3::timed_run(steps) (solver_v3.cu:285-298): runs `steps` steps and returns
+ * their elapsed GPU time in seconds, measured with CUDA events on the solver's stream. */
+int lbm_timed_run(lbm_solver* s, int steps, double* seconds);
+
+/* Waits for all work of s. */
+int lbm_synchronize(lbm_solver* s);
+
+/* Replaces SolverV3::populations() (solver_v3.cu:300-320): post-streaming populations in v0
+ * layout into s_host (nx*ny*9 values of the host type), solid cells 0. The gather runs on the
+ * device. */
+int lbm_get_populations(lbm_solver* s, void* s_host);
+
+/* Replaces SolverV3::macroscopic(rho, ux, uy) (solver_v3.cu:322-343): rho, ux, uy (nx*ny values
+ * each of the host type, row-major) with the Guo half-force velocity; solid cells 0. Computed by
+ * a device moment pass, bit-exact with v0 in the FP32 / FP64 forms. */
+int lbm_macroscopic(lbm_solver* s, void* rho, void* ux, void* uy);
+
+/* Replaces SolverV3::total_mass() (solver_v3.cu:345-355): fluid-cell count + sum of all fluid
+ * populations, accumulated in double on the device (fixed-order two-pass reduction; the
+ * summation order differs from v0 in the last bits, as the reference's v1 notes,
+ * src/v1_omp/solver_v1.cpp:221-222). */
+int lbm_total_mass(lbm_solver* s, double* mass);
+
+/* Replaces SolverV3::populations_at(x, y, out) (solver_v3.cu:234-249): the 9 post-streaming
+ * populations of cell (x, y) into out9 (host type). */
+int lbm_populations_at(lbm_solver* s, int x, int y, void* out9);
+
+/* Writes 1 to *finite if every population is finite, else 0 (device check). */
+int lbm_check_finite(lbm_solver* s, int* finite);
+
+/* Replaces SolverV3::bench_info() (solver_v3.cu:357-370): JSON fields (no braces) describing
+ * the device and the kernel configuration, written into buf (always NUL-terminated). */
+int lbm_device_info(lbm_solver* s, char* buf, size_t size);
+
+/* Geometry and precision of s (any pointer may be null). */
+int lbm_get_shape(const lbm_solver* s, int* nx, int* ny, int* precision);
+
+/* Kernel configuration of the step: threads per block and blocks (0 = automatic: a persistent
+ * grid of resident blocks). Used by the autotuner. */
+int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
+
+/* Device memory of the two population buffers (for zero-copy consumers): plane stride and row
+ * pitch in elements, and the current read buffer. */
+int lbm_state_view(lbm_solver* s, void** current, long long* plane_stride, int* row_pitch);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBM_B200_H */

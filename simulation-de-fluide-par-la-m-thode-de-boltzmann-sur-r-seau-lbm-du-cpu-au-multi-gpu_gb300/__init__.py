@@ -1,0 +1,225 @@
+"""GB300 (sm_103a) D2Q9 lattice-Boltzmann hot path: Python binding of the C ABI.
+
+`Solver` mirrors the member set of the reference's GPU solver lbm::SolverV3
+(src/v3_cuda_opt/solver_v3.hpp:27-57): construct from grid, tau, force and solid mask; then
+init_equilibrium / set_inflow_outflow / step / run / timed_run / macroscopic / total_mass /
+populations / populations_at / threads / bench_info / nx / ny / solid. Errors follow the
+reference: invalid arguments raise ValueError (std::invalid_argument there), CUDA failures raise
+RuntimeError (the reference aborts).
+
+The binding loads lib/liblbm_b200.so (built by build.py). There is no CPU fallback: without
+the library, or without a GPU, constructing a Solver raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from . import geometry  # noqa: F401  (re-exported)
+from .geometry import make_channel, make_cylinder, poiseuille_force  # noqa: F401
+
+_HERE = Path(__file__).resolve().parent
+LIB_PATH = _HERE / "lib" / "liblbm_b200.so"
+
+FP32, FP64, FP16_STORE, BF16_STORE = 0, 1, 2, 3
+PRECISIONS = {"fp32": FP32, "fp64": FP64, "fp16": FP16_STORE, "fp16_store": FP16_STORE,
+              "bf16": BF16_STORE, "bf16_store": BF16_STORE}
+HOST_DTYPE = {FP32: np.float32, FP64: np.float64, FP16_STORE: np.float32, BF16_STORE: np.float32}
+
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_DIVERGED, ERR_UNSUPPORTED = range(6)
+
+_lib = None
+
+
+def build(**kw) -> Path:
+    """Compiles the CUDA library (see build.py)."""
+    import importlib
+    return importlib.import_module(f"{__name__}.build").build(**kw)
+
+
+def lib() -> C.CDLL:
+    """The loaded C library (raises if it was not built)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise RuntimeError(f"CUDA library missing: {LIB_PATH} (run build())")
+        L = C.CDLL(str(LIB_PATH))
+        vp, i, d = C.c_void_p, C.c_int, C.c_double
+        sig = {
+            "lbm_version": ([], C.c_char_p),
+            "lbm_create": ([i, i, vp, d, d, d, i, C.POINTER(vp)], i),
+            "lbm_destroy": ([vp], i),
+            "lbm_last_error": ([vp], C.c_char_p),
+            "lbm_set_stream": ([vp, vp], i),
+            "lbm_set_inflow_outflow": ([vp, d], i),
+            "lbm_init_equilibrium": ([vp, d, d, d], i),
+            "lbm_set_populations": ([vp, vp], i),
+            "lbm_step": ([vp, i], i),
+            "lbm_run": ([vp, i], i),
+            "lbm_timed_run": ([vp, i, C.POINTER(d)], i),
+            "lbm_synchronize": ([vp], i),
+            "lbm_get_populations": ([vp, vp], i),
+            "lbm_macroscopic": ([vp, vp, vp, vp], i),
+            "lbm_total_mass": ([vp, C.POINTER(d)], i),
+            "lbm_populations_at": ([vp, i, i, vp], i),
+            "lbm_check_finite": ([vp, C.POINTER(i)], i),
+            "lbm_device_info": ([vp, C.c_char_p, C.c_size_t], i),
+            "lbm_get_shape": ([vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)], i),
+            "lbm_set_launch": ([vp, i, i], i),
+            "lbm_state_view": ([vp, C.POINTER(vp), C.POINTER(C.c_longlong), C.POINTER(i)], i),
+        }
+        for name, (args, res) in sig.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _ptr(a: np.ndarray) -> C.c_void_p:
+    return C.c_void_p(a.ctypes.data)
+
+
+class LbmError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"lbm error {code}: {msg}")
+        self.code = code
+
+
+def _raise(code: int, msg: str):
+    if code == ERR_INVALID_ARG:
+        raise ValueError(msg or "invalid argument")
+    raise LbmError(code, msg)
+
+
+class Solver:
+    """D2Q9 BGK + Guo + halfway bounce-back solver on one GPU (drop-in for lbm::SolverV3).
+
+    precision: "fp32" / "fp64" (bit-exact with the reference's v0 in float / double),
+    "fp16" / "bf16" (16-bit storage of g_i with per-plane scales, FP32 arithmetic).
+    Host arrays use the reference's v0 layout and the solver's host dtype (float32, or float64
+    for "fp64").
+    """
+
+    def __init__(self, nx: int, ny: int, tau: float, force_x: float, force_y: float, solid,
+                 precision="fp32"):
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.dtype = HOST_DTYPE[self.precision]
+        self._solid = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+        if self._solid.size != nx * ny:
+            raise ValueError("solid mask size does not match the grid")
+        self._nx, self._ny = int(nx), int(ny)
+        self.tau, self.fx, self.fy = float(tau), float(force_x), float(force_y)
+        self._h = C.c_void_p()
+        rc = lib().lbm_create(self._nx, self._ny, _ptr(self._solid), self.tau, self.fx, self.fy,
+                              self.precision, C.byref(self._h))
+        if rc != OK:
+            _raise(rc, "lbm_create failed (tau must be > 0.5, nx, ny >= 1)")
+
+    # -- lifetime ----------------------------------------------------------------------------
+    def close(self):
+        if self._h:
+            lib().lbm_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def _check(self, rc: int):
+        if rc != OK:
+            _raise(rc, (lib().lbm_last_error(self._h) or b"").decode())
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    # -- SolverV3 member set ------------------------------------------------------------------
+    def init_equilibrium(self, rho0: float, ux0: float, uy0: float):
+        self._check(lib().lbm_init_equilibrium(self._h, rho0, ux0, uy0))
+
+    def set_inflow_outflow(self, u_in: float):
+        self._check(lib().lbm_set_inflow_outflow(self._h, u_in))
+
+    def set_populations(self, s):
+        s = np.ascontiguousarray(s, dtype=self.dtype).reshape(-1)
+        if s.size != self._nx * self._ny * 9:
+            raise ValueError("populations must hold nx*ny*9 values")
+        self._check(lib().lbm_set_populations(self._h, _ptr(s)))
+
+    def step(self, steps: int = 1):
+        self._check(lib().lbm_step(self._h, steps))
+
+    def run(self, steps: int):
+        self._check(lib().lbm_run(self._h, steps))
+
+    def timed_run(self, steps: int) -> float:
+        t = C.c_double(0.0)
+        self._check(lib().lbm_timed_run(self._h, steps, C.byref(t)))
+        return t.value
+
+    def synchronize(self):
+        self._check(lib().lbm_synchronize(self._h))
+
+    def macroscopic(self, out=None):
+        n = self._nx * self._ny
+        rho, ux, uy = out if out is not None else (np.empty(n, self.dtype) for _ in range(3))
+        self._check(lib().lbm_macroscopic(self._h, _ptr(rho), _ptr(ux), _ptr(uy)))
+        return rho, ux, uy
+
+    def total_mass(self) -> float:
+        m = C.c_double(0.0)
+        self._check(lib().lbm_total_mass(self._h, C.byref(m)))
+        return m.value
+
+    def populations(self, out=None) -> np.ndarray:
+        out = np.empty(self._nx * self._ny * 9, self.dtype) if out is None else out
+        self._check(lib().lbm_get_populations(self._h, _ptr(out)))
+        return out
+
+    def populations_at(self, x: int, y: int) -> np.ndarray:
+        out = np.empty(9, self.dtype)
+        self._check(lib().lbm_populations_at(self._h, x, y, _ptr(out)))
+        return out
+
+    def check_finite(self) -> bool:
+        f = C.c_int(0)
+        self._check(lib().lbm_check_finite(self._h, C.byref(f)))
+        return bool(f.value)
+
+    def threads(self) -> int:
+        return 0
+
+    def bench_info(self) -> str:
+        buf = C.create_string_buffer(1024)
+        self._check(lib().lbm_device_info(self._h, buf, 1024))
+        return buf.value.decode()
+
+    def set_launch(self, block_threads: int, grid_blocks: int = 0):
+        self._check(lib().lbm_set_launch(self._h, block_threads, grid_blocks))
+
+    def set_stream(self, stream_handle: int):
+        self._check(lib().lbm_set_stream(self._h, C.c_void_p(stream_handle)))
+
+    def nx(self) -> int:
+        return self._nx
+
+    def ny(self) -> int:
+        return self._ny
+
+    def solid(self) -> np.ndarray:
+        return self._solid
+
+
+def version() -> str:
+    return lib().lbm_version().decode()

@@ -1,0 +1,286 @@
+// Device-side building blocks shared by the kernels of the library: arithmetic policies, the
+// storage codecs of the populations, 16-byte vector loads/stores, the bit-packed solid mask and
+// the kernel argument blocks.
+//
+// Data layout in HBM (one instance):
+//   populations  R[i][y][x] at  base + i * plane + y * pitch + x   (structure of arrays: 9 planes
+//                of shifted post-collision populations g_i = f_i - w_i, pull scheme). pitch is nx
+//                rounded up so that every row starts on a 128-byte boundary; plane = pitch * ny.
+//                Two such buffers (read / write), swapped every step.
+//   mask         uint32 words, mask_words per row, bit (x + 1) of row y = solid(x, y); bit 0 holds
+//                solid(nx - 1, y) and bit nx + 1 holds solid(0, y) (the periodic neighbours of the
+//                edge columns), bits beyond nx + 1 are 1. A thread that owns cells x0 .. x0+G-1
+//                extracts the G + 2 bits of cells x0 - 1 .. x0 + G with one funnel shift.
+#pragma once
+
+#include <cuda_bf16.h>
+#include <cuda_fp16.h>
+#include <cuda_runtime.h>
+
+#include <cstdint>
+
+#include "collide.h"
+
+namespace lbm_b200 {
+
+// ---------------------------------------------------------------------------------------------
+// Arithmetic policies
+// ---------------------------------------------------------------------------------------------
+// IEEE round-to-nearest operations that the compiler never contracts into FMA (CUDA's __f*_rn /
+// __d*_rn intrinsics). Used by the plain FP32/FP64 forms, which must match the reference bit for
+// bit. Host fallbacks keep the templates instantiable on the host side of the translation unit.
+struct ExactF32 {
+  using T = float;
+  static __host__ __device__ __forceinline__ float add(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fadd_rn(a, b);
+#else
+    return a + b;
+#endif
+  }
+  static __host__ __device__ __forceinline__ float sub(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fsub_rn(a, b);
+#else
+    return a - b;
+#endif
+  }
+  static __host__ __device__ __forceinline__ float mul(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fmul_rn(a, b);
+#else
+    return a * b;
+#endif
+  }
+  static __host__ __device__ __forceinline__ float div(float a, float b) {
+#ifdef __CUDA_ARCH__
+    return __fdiv_rn(a, b);
+#else
+    return a / b;
+#endif
+  }
+};
+
+struct ExactF64 {
+  using T = double;
+  static __host__ __device__ __forceinline__ double add(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dadd_rn(a, b);
+#else
+    return a + b;
+#endif
+  }
+  static __host__ __device__ __forceinline__ double sub(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dsub_rn(a, b);
+#else
+    return a - b;
+#endif
+  }
+  static __host__ __device__ __forceinline__ double mul(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __dmul_rn(a, b);
+#else
+    return a * b;
+#endif
+  }
+  static __host__ __device__ __forceinline__ double div(double a, double b) {
+#ifdef __CUDA_ARCH__
+    return __ddiv_rn(a, b);
+#else
+    return a / b;
+#endif
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
+// Storage codecs: stored type ST <-> compute type T. Plain forms store T itself; the 16-bit
+// forms store g_i * scale_i rounded to half / bfloat16, scale_i a power of two per plane.
+// ---------------------------------------------------------------------------------------------
+template <class ST>
+struct StoreTraits;
+template <>
+struct StoreTraits<float> {
+  using T = float;
+  static constexpr int kVec = 4;  // cells per 16-byte vector
+};
+template <>
+struct StoreTraits<double> {
+  using T = double;
+  static constexpr int kVec = 2;
+};
+template <>
+struct StoreTraits<__half> {
+  using T = float;
+  static constexpr int kVec = 8;
+};
+template <>
+struct StoreTraits<__nv_bfloat16> {
+  using T = float;
+  static constexpr int kVec = 8;
+};
+
+struct PlaneScales {
+  float enc[kQ];  // stored = g * enc[i]
+  float dec[kQ];  // g = stored * dec[i]
+};
+
+__device__ __forceinline__ float to_float(__half h) { return __half2float(h); }
+__device__ __forceinline__ float to_float(__nv_bfloat16 h) { return __bfloat162float(h); }
+template <class ST>
+__device__ __forceinline__ ST from_float(float v);
+template <>
+__device__ __forceinline__ __half from_float<__half>(float v) { return __float2half_rn(v); }
+template <>
+__device__ __forceinline__ __nv_bfloat16 from_float<__nv_bfloat16>(float v) {
+  return __float2bfloat16_rn(v);
+}
+
+// Scalar decode / encode of plane i.
+template <class ST>
+__device__ __forceinline__ typename StoreTraits<ST>::T decode(ST v, int, const PlaneScales&) {
+  return v;
+}
+template <>
+__device__ __forceinline__ float decode<__half>(__half v, int i, const PlaneScales& s) {
+  return to_float(v) * s.dec[i];
+}
+template <>
+__device__ __forceinline__ float decode<__nv_bfloat16>(__nv_bfloat16 v, int i,
+                                                       const PlaneScales& s) {
+  return to_float(v) * s.dec[i];
+}
+template <class ST>
+__device__ __forceinline__ ST encode(typename StoreTraits<ST>::T v, int, const PlaneScales&) {
+  return v;
+}
+template <>
+__device__ __forceinline__ __half encode<__half>(float v, int i, const PlaneScales& s) {
+  return from_float<__half>(v * s.enc[i]);
+}
+template <>
+__device__ __forceinline__ __nv_bfloat16 encode<__nv_bfloat16>(float v, int i,
+                                                               const PlaneScales& s) {
+  return from_float<__nv_bfloat16>(v * s.enc[i]);
+}
+
+// 16-byte vector load (read-only path) / store of kVec consecutive cells, decoded.
+template <class ST>
+__device__ __forceinline__ void load_vec(const ST* p, typename StoreTraits<ST>::T (&v)[StoreTraits<ST>::kVec],
+                                         int plane_index, const PlaneScales& s);
+template <>
+__device__ __forceinline__ void load_vec<float>(const float* p, float (&v)[4], int,
+                                                const PlaneScales&) {
+  const float4 t = __ldg(reinterpret_cast<const float4*>(p));
+  v[0] = t.x;
+  v[1] = t.y;
+  v[2] = t.z;
+  v[3] = t.w;
+}
+template <>
+__device__ __forceinline__ void load_vec<double>(const double* p, double (&v)[2], int,
+                                                 const PlaneScales&) {
+  const double2 t = __ldg(reinterpret_cast<const double2*>(p));
+  v[0] = t.x;
+  v[1] = t.y;
+}
+template <class H>
+__device__ __forceinline__ void load_vec16(const H* p, float (&v)[8], int i, const PlaneScales& s) {
+  const uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
+  const uint32_t w[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    H lo, hi;
+    const uint16_t a = static_cast<uint16_t>(w[k] & 0xffffu), b = static_cast<uint16_t>(w[k] >> 16);
+    memcpy(&lo, &a, 2);
+    memcpy(&hi, &b, 2);
+    v[2 * k] = to_float(lo) * s.dec[i];
+    v[2 * k + 1] = to_float(hi) * s.dec[i];
+  }
+}
+template <>
+__device__ __forceinline__ void load_vec<__half>(const __half* p, float (&v)[8], int i,
+                                                 const PlaneScales& s) {
+  load_vec16(p, v, i, s);
+}
+template <>
+__device__ __forceinline__ void load_vec<__nv_bfloat16>(const __nv_bfloat16* p, float (&v)[8],
+                                                        int i, const PlaneScales& s) {
+  load_vec16(p, v, i, s);
+}
+
+template <class ST>
+__device__ __forceinline__ void store_vec(ST* p, const typename StoreTraits<ST>::T (&v)[StoreTraits<ST>::kVec],
+                                          int plane_index, const PlaneScales& s);
+template <>
+__device__ __forceinline__ void store_vec<float>(float* p, const float (&v)[4], int,
+                                                 const PlaneScales&) {
+  *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+}
+template <>
+__device__ __forceinline__ void store_vec<double>(double* p, const double (&v)[2], int,
+                                                  const PlaneScales&) {
+  *reinterpret_cast<double2*>(p) = make_double2(v[0], v[1]);
+}
+template <class H>
+__device__ __forceinline__ void store_vec16(H* p, const float (&v)[8], int i, const PlaneScales& s) {
+  uint32_t w[4];
+#pragma unroll
+  for (int k = 0; k < 4; ++k) {
+    const H lo = from_float<H>(v[2 * k] * s.enc[i]);
+    const H hi = from_float<H>(v[2 * k + 1] * s.enc[i]);
+    uint16_t a, b;
+    memcpy(&a, &lo, 2);
+    memcpy(&b, &hi, 2);
+    w[k] = static_cast<uint32_t>(a) | (static_cast<uint32_t>(b) << 16);
+  }
+  *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+}
+template <>
+__device__ __forceinline__ void store_vec<__half>(__half* p, const float (&v)[8], int i,
+                                                  const PlaneScales& s) {
+  store_vec16(p, v, i, s);
+}
+template <>
+__device__ __forceinline__ void store_vec<__nv_bfloat16>(__nv_bfloat16* p, const float (&v)[8],
+                                                         int i, const PlaneScales& s) {
+  store_vec16(p, v, i, s);
+}
+
+template <class ST>
+__device__ __forceinline__ typename StoreTraits<ST>::T load_one(const ST* p, int i,
+                                                                const PlaneScales& s) {
+  return decode<ST>(__ldg(p), i, s);
+}
+
+// ---------------------------------------------------------------------------------------------
+// Bit-packed mask
+// ---------------------------------------------------------------------------------------------
+// Bits x0 .. x0+31 of a mask row (cells x0 - 1 .. x0 + 30).
+__device__ __forceinline__ uint32_t mask_window(const uint32_t* __restrict__ row, int x0) {
+  const int w = x0 >> 5;
+  return __funnelshift_r(__ldg(row + w), __ldg(row + w + 1), x0 & 31);
+}
+__device__ __forceinline__ bool mask_solid(const uint32_t* __restrict__ mask, int mask_words,
+                                           int x, int y) {
+  const uint32_t word = __ldg(mask + static_cast<size_t>(y) * mask_words + ((x + 1) >> 5));
+  return (word >> ((x + 1) & 31)) & 1u;
+}
+
+// ---------------------------------------------------------------------------------------------
+// Geometry of one instance on the device
+// ---------------------------------------------------------------------------------------------
+struct Grid2D {
+  int nx, ny, pitch;
+  int mask_words;
+  long long plane;  // elements per population plane (pitch * ny)
+  int open_x;
+};
+
+// Nine values passed by value as a kernel parameter (inlet or initial equilibrium).
+template <class T>
+struct Eq9 {
+  T v[kQ];
+};
+
+}  // namespace lbm_b200

@@ -1,0 +1,600 @@
+// Single-grid solver: device memory, launches and the C ABI of include/lbm_b200.h.
+//
+// Host code of this file is compiled with -ffp-contract=off: the per-launch constants (omega,
+// the force prefactor, the inlet and initial equilibria) are computed here in the solver
+// precision with the reference's expressions, and must round exactly as the reference's host
+// code does (src/v3_cuda_opt/solver_v3.cu:194-226,252-253).
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "aux_kernels.cuh"
+#include "lbm_b200.h"
+#include "solver_internal.h"
+#include "step_kernel.cuh"
+
+using namespace lbm_b200;
+
+namespace {
+
+template <class ST>
+struct Form;
+template <>
+struct Form<float> {
+  using A = ExactF32;
+  using Phys = ExactPhys<ExactF32>;
+  static constexpr const char* name = "fp32";
+};
+template <>
+struct Form<double> {
+  using A = ExactF64;
+  using Phys = ExactPhys<ExactF64>;
+  static constexpr const char* name = "fp64";
+};
+template <>
+struct Form<__half> {
+  using A = ExactF32;
+  using Phys = ExactPhys<ExactF32>;
+  static constexpr const char* name = "fp16_store";
+};
+template <>
+struct Form<__nv_bfloat16> {
+  using A = ExactF32;
+  using Phys = ExactPhys<ExactF32>;
+  static constexpr const char* name = "bf16_store";
+};
+
+constexpr int kCx[kQ] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+constexpr int kCy[kQ] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+
+// Shifted equilibrium of (rho0, ux0, uy0) in T, the reference's expressions and order
+// (src/common/boundary.hpp:26-34, src/common/d2q9.hpp:40-42).
+template <class T>
+Eq9<T> host_equilibrium(T rho0, T ux0, T uy0) {
+  Eq9<T> e{};
+  const T usq = ux0 * ux0 + uy0 * uy0;
+  const T drho0 = rho0 - T(1);
+  for (int i = 0; i < kQ; ++i) {
+    const T cu = kCx[i] * ux0 + kCy[i] * uy0;
+    e.v[i] = weight<T>(i) * (drho0 + rho0 * (T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq));
+  }
+  return e;
+}
+
+int set_error(lbm_solver* s, int code, const std::string& msg) {
+  if (s) s->err = msg;
+  return code;
+}
+
+int cuda_fail(lbm_solver* s, cudaError_t e, const char* what) {
+  cudaGetLastError();  // clear a sticky launch error so that later calls can report their own
+  const int code = e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA;
+  return set_error(s, code, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+#define LBM_CUDA(s, call)                                   \
+  do {                                                      \
+    const cudaError_t lbm_e_ = (call);                      \
+    if (lbm_e_ != cudaSuccess) return cuda_fail(s, lbm_e_, #call); \
+  } while (0)
+
+int grid_for_cells(const lbm_solver* s, long long n, int block) {
+  const long long want = (n + block - 1) / block;
+  return static_cast<int>(std::max<long long>(1, std::min<long long>(want, 32LL * s->sm_count)));
+}
+
+template <class ST>
+Eq9<typename StoreTraits<ST>::T> inlet_eq(const lbm_solver* s) {
+  using T = typename StoreTraits<ST>::T;
+  if (!s->open_x) return Eq9<T>{};
+  return host_equilibrium<T>(T(1), T(s->u_in), T(0));
+}
+
+template <class ST, bool kOpen>
+int launch_steps_t(lbm_solver* s, int steps) {
+  using Phys = typename Form<ST>::Phys;
+  using T = typename StoreTraits<ST>::T;
+  constexpr int G = StoreTraits<ST>::kVec;
+  StepArgs<ST, Phys> a{};
+  a.mask = s->mask_d;
+  a.g = s->g;
+  a.cpr = (s->nx + 32 * G - 1) / (32 * G);
+  a.items = s->ny * a.cpr;
+  a.k = make_collide_consts<T>(T(s->tau), T(s->fx), T(s->fy));
+  const Eq9<T> e = inlet_eq<ST>(s);
+  for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
+  a.sc = s->sc;
+  const auto kernel = pull_step_kernel<ST, Phys, kOpen>;
+  int grid = s->grid;
+  if (grid <= 0) {
+    int per_sm = 0;
+    LBM_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, s->block, 0));
+    const int warps_per_block = s->block / 32;
+    const int need = (a.items + warps_per_block - 1) / warps_per_block;
+    grid = std::max(1, std::min(need, std::max(1, per_sm) * s->sm_count));
+  }
+  s->last_grid = grid;
+  for (int k = 0; k < steps; ++k) {
+    a.src = static_cast<const ST*>(s->buf[s->cur]);
+    a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+    kernel<<<grid, s->block, 0, s->stream>>>(a);
+    s->cur ^= 1;
+  }
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int launch_steps(lbm_solver* s, int steps) {
+  return s->open_x ? launch_steps_t<ST, true>(s, steps) : launch_steps_t<ST, false>(s, steps);
+}
+
+template <class ST>
+int set_state_t(lbm_solver* s, const void* aos_dev, Eq9<typename StoreTraits<ST>::T> eq) {
+  using T = typename StoreTraits<ST>::T;
+  const long long n = static_cast<long long>(s->nx) * s->ny;
+  const int grid = grid_for_cells(s, n, 256);
+  // Both buffers: the step never writes solid cells of an all-solid chunk, so they must hold 0
+  // in the buffer it writes too (cudaMemset at creation); the current one gets the state.
+  set_state_kernel<ST><<<grid, 256, 0, s->stream>>>(static_cast<ST*>(s->buf[s->cur]), s->mask_d,
+                                                    s->g, static_cast<const T*>(aos_dev), eq,
+                                                    s->sc);
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int get_state_t(lbm_solver* s, void* aos_dev) {
+  using T = typename StoreTraits<ST>::T;
+  const long long n = static_cast<long long>(s->nx) * s->ny;
+  get_state_kernel<ST><<<grid_for_cells(s, n, 256), 256, 0, s->stream>>>(
+      static_cast<const ST*>(s->buf[s->cur]), s->mask_d, s->g, inlet_eq<ST>(s), s->sc,
+      static_cast<T*>(aos_dev));
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int moments_t(lbm_solver* s, void* rho, void* ux, void* uy) {
+  using A = typename Form<ST>::A;
+  using T = typename A::T;
+  const long long n = static_cast<long long>(s->nx) * s->ny;
+  const T hfx = T(0.5) * T(s->fx), hfy = T(0.5) * T(s->fy);
+  moments_kernel<ST, A><<<grid_for_cells(s, n, 256), 256, 0, s->stream>>>(
+      static_cast<const ST*>(s->buf[s->cur]), s->mask_d, s->g, inlet_eq<ST>(s), s->sc, hfx, hfy,
+      static_cast<T*>(rho), static_cast<T*>(ux), static_cast<T*>(uy));
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int mass_t(lbm_solver* s, const void* state, double* partials, int blocks, double* out) {
+  mass_partial_kernel<ST><<<blocks, kReduceThreads, 0, s->stream>>>(
+      static_cast<const ST*>(state), s->mask_d, s->g, inlet_eq<ST>(s), s->sc, partials);
+  mass_final_kernel<<<1, kReduceThreads, 0, s->stream>>>(partials, blocks,
+                                                         static_cast<double>(s->fluid), out);
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int finite_t(lbm_solver* s, int* flag) {
+  const long long n = static_cast<long long>(s->nx) * s->ny;
+  finite_kernel<ST><<<grid_for_cells(s, n, 256), 256, 0, s->stream>>>(
+      static_cast<const ST*>(s->buf[s->cur]), s->mask_d, s->g, s->sc, flag);
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int probe_t(lbm_solver* s, int x, int y, void* out) {
+  using T = typename StoreTraits<ST>::T;
+  probe_kernel<ST><<<1, 32, 0, s->stream>>>(static_cast<const ST*>(s->buf[s->cur]), s->mask_d,
+                                            s->g, inlet_eq<ST>(s), s->sc, x, y,
+                                            static_cast<T*>(out));
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+// Dispatch on the storage form (one code path per form, no fallback).
+#define LBM_DISPATCH(s, fn, ...)                                       \
+  switch ((s)->precision) {                                           \
+    case LBM_FP32: return fn<float>(__VA_ARGS__);                     \
+    case LBM_FP64: return fn<double>(__VA_ARGS__);                    \
+    case LBM_FP16_STORE: return fn<__half>(__VA_ARGS__);              \
+    case LBM_BF16_STORE: return fn<__nv_bfloat16>(__VA_ARGS__);       \
+    default: return set_error(s, LBM_ERR_INVALID_ARG, "bad precision"); \
+  }
+
+template <class ST>
+int init_eq_t(lbm_solver* s, double rho0, double ux0, double uy0) {
+  using T = typename StoreTraits<ST>::T;
+  return set_state_t<ST>(s, nullptr, host_equilibrium<T>(T(rho0), T(ux0), T(uy0)));
+}
+
+int ensure_stage(lbm_solver* s, size_t bytes) {
+  if (s->stage_bytes >= bytes) return LBM_OK;
+  if (s->stage) {
+    LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+    cudaFree(s->stage);
+    s->stage = nullptr;
+    s->stage_bytes = 0;
+  }
+  LBM_CUDA(s, cudaMalloc(&s->stage, bytes));
+  s->stage_bytes = bytes;
+  return LBM_OK;
+}
+
+int check(const lbm_solver* s) { return s ? LBM_OK : LBM_ERR_INVALID_ARG; }
+
+// Per-plane power-of-two scales of the 16-bit forms: the largest stored magnitude 65504 / scale
+// is 2 for the rest population, 0.5 for the axis and 0.25 for the diagonal ones, which holds
+// g_i = w_i [drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2)] for |u| <= 0.3 and |drho| <= 0.5 with the
+// smallest values of interest (~1e-9) still above the FP16 subnormal range.
+PlaneScales default_scales(int precision) {
+  PlaneScales p{};
+  for (int i = 0; i < kQ; ++i) {
+    const int e = precision == LBM_FP16_STORE || precision == LBM_BF16_STORE
+                      ? (i == 0 ? 15 : (i <= 4 ? 17 : 18))
+                      : 0;
+    p.enc[i] = std::ldexp(1.0f, e);
+    p.dec[i] = std::ldexp(1.0f, -e);
+  }
+  return p;
+}
+
+}  // namespace
+
+// ----------------------------------------------------------------------------------------------
+// Internal helpers shared with the other translation units
+// ----------------------------------------------------------------------------------------------
+namespace lbm_b200 {
+
+int solver_step_raw(lbm_solver* s, int steps) { LBM_DISPATCH(s, launch_steps, s, steps); }
+
+int solver_mass_into(lbm_solver* s, const void* state, double* partials, int blocks,
+                     double* out) {
+  LBM_DISPATCH(s, mass_t, s, state, partials, blocks, out);
+}
+
+void pack_mask(const uint8_t* solid, int nx, int ny, int mask_words, std::vector<uint32_t>& out) {
+  out.assign(static_cast<size_t>(mask_words) * ny, 0xffffffffu);
+  for (int y = 0; y < ny; ++y) {
+    uint32_t* row = out.data() + static_cast<size_t>(y) * mask_words;
+    const uint8_t* src = solid + static_cast<size_t>(y) * nx;
+    auto set = [&](int bit, bool v) {
+      if (v)
+        row[bit >> 5] |= 1u << (bit & 31);
+      else
+        row[bit >> 5] &= ~(1u << (bit & 31));
+    };
+    set(0, src[nx - 1] != 0);
+    for (int x = 0; x < nx; ++x) set(x + 1, src[x] != 0);
+    set(nx + 1, src[0] != 0);
+  }
+}
+
+int element_bytes(int precision) {
+  switch (precision) {
+    case LBM_FP32: return 4;
+    case LBM_FP64: return 8;
+    case LBM_FP16_STORE:
+    case LBM_BF16_STORE: return 2;
+    default: return 0;
+  }
+}
+
+}  // namespace lbm_b200
+
+// ----------------------------------------------------------------------------------------------
+// C ABI
+// ----------------------------------------------------------------------------------------------
+extern "C" {
+
+const char* lbm_version(void) { return "lbm_b200 1.0 (sm_103a)"; }
+
+int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, double fy,
+               int precision, lbm_solver** out) {
+  if (!out) return LBM_ERR_INVALID_ARG;
+  *out = nullptr;
+  const int elem = element_bytes(precision);
+  if (nx < 1 || ny < 1 || !solid || elem == 0) return LBM_ERR_INVALID_ARG;
+  // The reference compares tau in its own precision (solver_v3.cu:169-170).
+  const bool tau_ok = precision == LBM_FP64 ? tau > 0.5 : static_cast<float>(tau) > 0.5f;
+  if (!tau_ok || !std::isfinite(tau) || !std::isfinite(fx) || !std::isfinite(fy))
+    return LBM_ERR_INVALID_ARG;
+  if (static_cast<long long>(nx) * ny > (1LL << 31) - 1) return LBM_ERR_INVALID_ARG;
+
+  lbm_solver* s = new (std::nothrow) lbm_solver();
+  if (!s) return LBM_ERR_OUT_OF_MEMORY;
+  s->nx = nx;
+  s->ny = ny;
+  s->precision = precision;
+  s->elem = elem;
+  s->vec = 16 / elem;
+  s->host_elem = precision == LBM_FP64 ? 8 : 4;
+  s->tau = tau;
+  s->fx = fx;
+  s->fy = fy;
+  s->solid.assign(solid, solid + static_cast<size_t>(nx) * ny);
+  for (uint8_t v : s->solid) s->fluid += v ? 0 : 1;
+  s->sc = default_scales(precision);
+
+  const int per_line = 128 / elem;
+  const int pitch = (nx + per_line - 1) / per_line * per_line;
+  const int cpr = (nx + 32 * s->vec - 1) / (32 * s->vec);
+  s->g.nx = nx;
+  s->g.ny = ny;
+  s->g.pitch = pitch;
+  s->g.mask_words = cpr * s->vec + 2;
+  s->g.plane = static_cast<long long>(pitch) * ny;
+  s->g.open_x = 0;
+
+  auto fail = [&](int code) {
+    lbm_destroy(s);
+    return code;
+  };
+  cudaError_t e = cudaGetDevice(&s->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
+  e = cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
+  s->own_stream = true;
+  e = cudaEventCreate(&s->ev[0]);
+  if (e == cudaSuccess) e = cudaEventCreate(&s->ev[1]);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
+
+  const size_t state_bytes = static_cast<size_t>(kQ) * s->g.plane * elem + 256;
+  for (int b = 0; b < 2; ++b) {
+    e = cudaMalloc(&s->buf[b], state_bytes);
+    if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
+    e = cudaMemsetAsync(s->buf[b], 0, state_bytes, s->stream);
+    if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
+  }
+  s->state_bytes = state_bytes;
+  std::vector<uint32_t> words;
+  pack_mask(solid, nx, ny, s->g.mask_words, words);
+  e = cudaMalloc(&s->mask_d, words.size() * sizeof(uint32_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(s->mask_d, words.data(), words.size() * sizeof(uint32_t),
+                        cudaMemcpyHostToDevice, s->stream);
+  if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
+  s->red_blocks = 4 * s->sm_count;
+  e = cudaMalloc(&s->red, (s->red_blocks + 2) * sizeof(double) + 2 * sizeof(int));
+  if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
+  e = cudaStreamSynchronize(s->stream);
+  if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
+  *out = s;
+  return LBM_OK;
+}
+
+int lbm_destroy(lbm_solver* s) {
+  if (!s) return LBM_OK;
+  if (s->stream) cudaStreamSynchronize(s->stream);
+  for (void* p : s->buf) cudaFree(p);
+  cudaFree(s->mask_d);
+  cudaFree(s->red);
+  cudaFree(s->stage);
+  for (cudaEvent_t ev : s->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (s->own_stream && s->stream) cudaStreamDestroy(s->stream);
+  delete s;
+  return LBM_OK;
+}
+
+const char* lbm_last_error(const lbm_solver* s) { return s ? s->err.c_str() : "null solver"; }
+
+int lbm_set_stream(lbm_solver* s, void* stream) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  if (s->own_stream) cudaStreamDestroy(s->stream);
+  s->own_stream = false;
+  s->stream = static_cast<cudaStream_t>(stream);
+  return LBM_OK;
+}
+
+int lbm_set_inflow_outflow(lbm_solver* s, double u_in) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  if (s->nx < 3 || !std::isfinite(u_in))
+    return set_error(s, LBM_ERR_INVALID_ARG, "open boundaries need nx >= 3 and a finite u_in");
+  s->open_x = true;
+  s->u_in = u_in;
+  s->g.open_x = 1;
+  return LBM_OK;
+}
+
+int lbm_init_equilibrium(lbm_solver* s, double rho0, double ux0, double uy0) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  LBM_DISPATCH(s, init_eq_t, s, rho0, ux0, uy0);
+}
+
+int lbm_set_populations(lbm_solver* s, const void* s_host) {
+  if (check(s) || !s_host) return set_error(s, LBM_ERR_INVALID_ARG, "null state");
+  const size_t bytes = static_cast<size_t>(s->nx) * s->ny * kQ * s->host_elem;
+  if (int rc = ensure_stage(s, bytes)) return rc;
+  LBM_CUDA(s, cudaMemcpyAsync(s->stage, s_host, bytes, cudaMemcpyHostToDevice, s->stream));
+  int rc;
+  switch (s->precision) {
+    case LBM_FP32: rc = set_state_t<float>(s, s->stage, Eq9<float>{}); break;
+    case LBM_FP64: rc = set_state_t<double>(s, s->stage, Eq9<double>{}); break;
+    case LBM_FP16_STORE: rc = set_state_t<__half>(s, s->stage, Eq9<float>{}); break;
+    case LBM_BF16_STORE: rc = set_state_t<__nv_bfloat16>(s, s->stage, Eq9<float>{}); break;
+    default: rc = LBM_ERR_INVALID_ARG;
+  }
+  if (rc) return rc;
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));  // the host buffer may be reused on return
+  return LBM_OK;
+}
+
+int lbm_step(lbm_solver* s, int steps) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  if (steps < 0) return set_error(s, LBM_ERR_INVALID_ARG, "steps must be >= 0");
+  if (steps == 0) return LBM_OK;
+  return lbm_b200::solver_step_raw(s, steps);
+}
+
+int lbm_synchronize(lbm_solver* s) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_run(lbm_solver* s, int steps) {
+  if (int rc = lbm_step(s, steps)) return rc;
+  return lbm_synchronize(s);
+}
+
+int lbm_timed_run(lbm_solver* s, int steps, double* seconds) {
+  if (check(s) || !seconds) return set_error(s, LBM_ERR_INVALID_ARG, "null argument");
+  LBM_CUDA(s, cudaEventRecord(s->ev[0], s->stream));
+  if (int rc = lbm_step(s, steps)) return rc;
+  LBM_CUDA(s, cudaEventRecord(s->ev[1], s->stream));
+  LBM_CUDA(s, cudaEventSynchronize(s->ev[1]));
+  float ms = 0.f;
+  LBM_CUDA(s, cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
+  *seconds = static_cast<double>(ms) * 1e-3;
+  return LBM_OK;
+}
+
+int lbm_get_populations(lbm_solver* s, void* s_host) {
+  if (check(s) || !s_host) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
+  const size_t bytes = static_cast<size_t>(s->nx) * s->ny * kQ * s->host_elem;
+  if (int rc = ensure_stage(s, bytes)) return rc;
+  int rc;
+  switch (s->precision) {
+    case LBM_FP32: rc = get_state_t<float>(s, s->stage); break;
+    case LBM_FP64: rc = get_state_t<double>(s, s->stage); break;
+    case LBM_FP16_STORE: rc = get_state_t<__half>(s, s->stage); break;
+    case LBM_BF16_STORE: rc = get_state_t<__nv_bfloat16>(s, s->stage); break;
+    default: rc = LBM_ERR_INVALID_ARG;
+  }
+  if (rc) return rc;
+  LBM_CUDA(s, cudaMemcpyAsync(s_host, s->stage, bytes, cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_macroscopic(lbm_solver* s, void* rho, void* ux, void* uy) {
+  if (check(s) || !rho || !ux || !uy) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
+  const size_t n = static_cast<size_t>(s->nx) * s->ny;
+  const size_t plane = n * s->host_elem;
+  if (int rc = ensure_stage(s, std::max(3 * plane, n * kQ * s->host_elem))) return rc;
+  char* d = static_cast<char*>(s->stage);
+  int rc;
+  switch (s->precision) {
+    case LBM_FP32: rc = moments_t<float>(s, d, d + plane, d + 2 * plane); break;
+    case LBM_FP64: rc = moments_t<double>(s, d, d + plane, d + 2 * plane); break;
+    case LBM_FP16_STORE: rc = moments_t<__half>(s, d, d + plane, d + 2 * plane); break;
+    case LBM_BF16_STORE: rc = moments_t<__nv_bfloat16>(s, d, d + plane, d + 2 * plane); break;
+    default: rc = LBM_ERR_INVALID_ARG;
+  }
+  if (rc) return rc;
+  LBM_CUDA(s, cudaMemcpyAsync(rho, d, plane, cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaMemcpyAsync(ux, d + plane, plane, cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaMemcpyAsync(uy, d + 2 * plane, plane, cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_total_mass(lbm_solver* s, double* mass) {
+  if (check(s) || !mass) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
+  double* out = s->red + s->red_blocks;
+  if (int rc = lbm_b200::solver_mass_into(s, s->buf[s->cur], s->red, s->red_blocks, out)) return rc;
+  LBM_CUDA(s, cudaMemcpyAsync(mass, out, sizeof(double), cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_populations_at(lbm_solver* s, int x, int y, void* out9) {
+  if (check(s) || !out9) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
+  if (x < 0 || x >= s->nx || y < 0 || y >= s->ny)
+    return set_error(s, LBM_ERR_INVALID_ARG, "cell outside the grid");
+  if (int rc = ensure_stage(s, kQ * 8)) return rc;
+  int rc;
+  switch (s->precision) {
+    case LBM_FP32: rc = probe_t<float>(s, x, y, s->stage); break;
+    case LBM_FP64: rc = probe_t<double>(s, x, y, s->stage); break;
+    case LBM_FP16_STORE: rc = probe_t<__half>(s, x, y, s->stage); break;
+    case LBM_BF16_STORE: rc = probe_t<__nv_bfloat16>(s, x, y, s->stage); break;
+    default: rc = LBM_ERR_INVALID_ARG;
+  }
+  if (rc) return rc;
+  LBM_CUDA(s, cudaMemcpyAsync(out9, s->stage, kQ * s->host_elem, cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_check_finite(lbm_solver* s, int* finite) {
+  if (check(s) || !finite) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
+  int* flag = reinterpret_cast<int*>(s->red + s->red_blocks + 2);
+  LBM_CUDA(s, cudaMemsetAsync(flag, 0, sizeof(int), s->stream));
+  int rc;
+  switch (s->precision) {
+    case LBM_FP32: rc = finite_t<float>(s, flag); break;
+    case LBM_FP64: rc = finite_t<double>(s, flag); break;
+    case LBM_FP16_STORE: rc = finite_t<__half>(s, flag); break;
+    case LBM_BF16_STORE: rc = finite_t<__nv_bfloat16>(s, flag); break;
+    default: rc = LBM_ERR_INVALID_ARG;
+  }
+  if (rc) return rc;
+  int bad = 0;
+  LBM_CUDA(s, cudaMemcpyAsync(&bad, flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  *finite = bad ? 0 : 1;
+  return LBM_OK;
+}
+
+int lbm_device_info(lbm_solver* s, char* buf, size_t size) {
+  if (check(s) || !buf || size == 0) return set_error(s, LBM_ERR_INVALID_ARG, "null buffer");
+  cudaDeviceProp prop{};
+  int driver = 0, runtime = 0;
+  LBM_CUDA(s, cudaGetDeviceProperties(&prop, s->device));
+  LBM_CUDA(s, cudaDriverGetVersion(&driver));
+  LBM_CUDA(s, cudaRuntimeGetVersion(&runtime));
+  auto ver = [](int v) { return std::to_string(v / 1000) + "." + std::to_string((v % 1000) / 10); };
+  static const char* names[] = {"fp32", "fp64", "fp16_store", "bf16_store"};
+  const std::string info =
+      "\"gpu\": \"" + std::string(prop.name) + "\", \"gpu_driver_cuda\": \"" + ver(driver) +
+      "\", \"cuda_runtime\": \"" + ver(runtime) + "\", \"cuda_compiled\": \"" +
+      ver(CUDART_VERSION) + "\", \"ecc\": " + std::to_string(prop.ECCEnabled) +
+      ", \"sm_count\": " + std::to_string(s->sm_count) + ", \"block\": \"" +
+      std::to_string(s->block) + "x1\", \"grid\": " + std::to_string(s->last_grid) +
+      ", \"variant\": \"b200_pull_vec" + std::to_string(s->vec) + "\", \"precision\": \"" +
+      names[s->precision] + "\"";
+  std::snprintf(buf, size, "%s", info.c_str());
+  return LBM_OK;
+}
+
+int lbm_get_shape(const lbm_solver* s, int* nx, int* ny, int* precision) {
+  if (!s) return LBM_ERR_INVALID_ARG;
+  if (nx) *nx = s->nx;
+  if (ny) *ny = s->ny;
+  if (precision) *precision = s->precision;
+  return LBM_OK;
+}
+
+int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  if (block_threads <= 0) block_threads = kStepThreads;
+  if (block_threads % 32 != 0 || block_threads > kStepThreads || grid_blocks < 0)
+    return set_error(s, LBM_ERR_INVALID_ARG, "block must be a multiple of 32 and <= 256");
+  s->block = block_threads;
+  s->grid = grid_blocks;
+  return LBM_OK;
+}
+
+int lbm_state_view(lbm_solver* s, void** current, long long* plane_stride, int* row_pitch) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  if (current) *current = s->buf[s->cur];
+  if (plane_stride) *plane_stride = s->g.plane;
+  if (row_pitch) *row_pitch = s->g.pitch;
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,82 @@
+// Host check of the simplified exact collision (csrc/collide.h) against the literal collision
+// of the reference's v0 (src/v0_cpu/solver_v0.cpp:86-99,127-143, src/common/d2q9.hpp:40-50),
+// on random states, in float and double. Exit status 0 when every output value is equal.
+// Compile with -ffp-contract=off.
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <random>
+
+#include "collide.h"
+
+namespace {
+
+constexpr int CX[9] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
+constexpr int CY[9] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+
+template <class T>
+void literal(const T* g, T omega, T fp, T fx, T fy, T* out) {
+  T m0 = 0, mx = 0, my = 0;
+  for (int i = 0; i < 9; ++i) {
+    m0 += g[i];
+    mx += CX[i] * g[i];
+    my += CY[i] * g[i];
+  }
+  const T drho = m0, rho = T(1) + drho;
+  const T ux = (mx + T(0.5) * fx) / rho, uy = (my + T(0.5) * fy) / rho;
+  const T usq = ux * ux + uy * uy;
+  for (int i = 0; i < 9; ++i) {
+    const T wi = lbm_b200::weight<T>(i);
+    const T cu = CX[i] * ux + CY[i] * uy;
+    const T geq = wi * (drho + rho * (T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq));
+    const T cxi = T(CX[i]), cyi = T(CY[i]);
+    const T cu2 = cxi * ux + cyi * uy, cf = cxi * fx + cyi * fy;
+    const T guo = wi * (T(3) * ((cxi - ux) * fx + (cyi - uy) * fy) + T(9) * cu2 * cf);
+    out[i] = g[i] - omega * (g[i] - geq) + fp * guo;
+  }
+}
+
+template <class T>
+long check(long trials, unsigned seed) {
+  std::mt19937_64 rng(seed);
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  long bad = 0;
+  for (long t = 0; t < trials; ++t) {
+    const double scale = std::pow(10.0, -1.0 - 5.0 * (0.5 + 0.5 * u(rng)));  // 1e-1 .. 1e-6
+    T g[9];
+    for (int i = 0; i < 9; ++i) g[i] = T(scale * u(rng) * lbm_b200::weight<double>(i) * 9.0);
+    if (t % 7 == 0) g[t % 9] = T(0);
+    const T tau = T(0.5 + 1e-3 + 1.5 * (0.5 + 0.5 * u(rng)));
+    T fx = T(1e-4 * u(rng)), fy = T(1e-4 * u(rng));
+    if (t % 5 == 0) fy = T(0);
+    if (t % 11 == 0) fx = T(0);
+    const auto k = lbm_b200::make_collide_consts<T>(tau, fx, fy);
+    T a[9], b[9];
+    literal<T>(g, k.omega, k.force_prefactor, fx, fy, a);
+    lbm_b200::collide_exact<lbm_b200::HostArith<T>>(g, k, b);
+    for (int i = 0; i < 9; ++i)
+      if (!(a[i] == b[i])) {
+        if (bad < 5)
+          std::printf("mismatch trial %ld dir %d: %.17g vs %.17g\n", t, i, (double)a[i], (double)b[i]);
+        ++bad;
+      }
+    // moments
+    T r1, u1, v1;
+    lbm_b200::moments_exact<lbm_b200::HostArith<T>>(g, k.hfx, k.hfy, r1, u1, v1);
+    T m0 = 0, mx = 0, my = 0;
+    for (int i = 0; i < 9; ++i) { m0 += g[i]; mx += CX[i] * g[i]; my += CY[i] * g[i]; }
+    const T rho = T(1) + m0;
+    if (!(r1 == rho && u1 == (mx + T(0.5) * fx) / rho && v1 == (my + T(0.5) * fy) / rho)) ++bad;
+  }
+  return bad;
+}
+
+}  // namespace
+
+int main(int argc, char** argv) {
+  const long trials = argc > 1 ? std::atol(argv[1]) : 100000;
+  const long bf = check<float>(trials, 1), bd = check<double>(trials, 2);
+  std::printf("collide_exact vs literal v0: float %ld / double %ld mismatching values in %ld states\n",
+              bf, bd, trials);
+  return (bf == 0 && bd == 0) ? 0 : 1;
+}
