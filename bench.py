@@ -128,7 +128,7 @@ class ClockSampler:
 
         sm = [num(r[0]) for r in inside if num(r[0]) is not None]
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        reasons = sorted({names[k] for r in inside for k in range(4) if "Active" in r[4 + k]})
+        reasons = sorted({names[k] for r in inside for k in range(4) if r[4 + k] == "Active"})
         return {"sm_mhz": statistics.median(sm) if sm else None,
                 "sm_max_mhz": num(inside[0][1]), "reasons": reasons, "samples": len(inside),
                 "power_w_median": statistics.median([num(r[2]) for r in inside if num(r[2])] or [0])}
@@ -179,25 +179,23 @@ def time_form(pkg, mask, s0, n, precision, steps, warmup):
 
 
 def cpu_baseline(orc, n: int, budget_s: float = 8.0):
-    """Oracle port of the reference's v1 solver (OpenMP, all host threads), bounded sample."""
+    """Oracle port of the reference's v1 solver (OpenMP, all host threads), bounded sample:
+    the full grid, as many steps as fit in about budget_s seconds (at most 50)."""
     threads = os.cpu_count() or 1
-    rows = n
-    mask = np.zeros(n * rows, np.uint8)
+    mask = np.zeros(n * n, np.uint8)
     mask[:n] = 1
     mask[-n:] = 1
-    s0 = orc.seeded_state(SEED, AMP, n, rows, mask, "f32")
-    r = orc.s_to_r(n, rows, mask, s0, real="f32")
-    del s0
+    bufs = orc.PullBuffers(n, n, mask, orc.s_to_r(n, n, mask, orc.seeded_state(SEED, AMP, n, n, mask)))
     t0 = time.perf_counter()
-    orc.pull_run(n, rows, mask, TAU, FX, FY, r, 1, real="f32", threads=threads)
+    bufs.run(TAU, FX, FY, 1, threads=threads)
     one = time.perf_counter() - t0
     steps = int(max(1, min(50, budget_s / max(one, 1e-6))))
     t0 = time.perf_counter()
-    orc.pull_run(n, rows, mask, TAU, FX, FY, r, steps, real="f32", threads=threads)
+    bufs.run(TAU, FX, FY, steps, threads=threads)
     dt = time.perf_counter() - t0
-    return {"value": n * rows * steps / dt / 1e6, "unit": "MLUPS", "cores": threads,
+    return {"value": round(n * n * steps / dt / 1e6, 2), "unit": "MLUPS", "cores": threads,
             "kind": "port",
-            "sample": f"{n}x{rows} walled channel, {steps} steps after 1 warm-up step, FP32, "
+            "sample": f"{n}x{n} walled channel, {steps} steps after 1 warm-up step, FP32, "
                       f"oracle pull port of reference v1 (src/v1_omp/solver_v1.cpp), "
                       f"{threads} OpenMP threads"}
 
@@ -329,26 +327,28 @@ def run_reference(args):
     warmup = max(args.warmup, 3)
     # Each bench step is one lattice step; the grid keeps all 4096 columns but its rows are
     # bounded so that warm-up + timed steps stay within about two minutes.
-    mask_full_row = np.ones(n, np.uint8)
-    rows = n
+    def channel(rows):
+        m = np.zeros(n * rows, np.uint8)
+        m[:n] = 1
+        m[-n:] = 1
+        return m
+
     probe_rows = 256
-    pm = np.zeros(n * probe_rows, np.uint8)
-    pm[:n] = 1
-    pm[-n:] = 1
-    pr = orc.s_to_r(n, probe_rows, pm, orc.seeded_state(SEED, AMP, n, probe_rows, pm, "f32"))
+    pm = channel(probe_rows)
+    pb = orc.PullBuffers(n, probe_rows, pm, orc.s_to_r(n, probe_rows, pm, orc.seeded_state(SEED, AMP, n, probe_rows, pm)))
+    pb.run(TAU, FX, FY, 1, threads=threads)
     t0 = time.perf_counter()
-    orc.pull_run(n, probe_rows, pm, TAU, FX, FY, pr, 2, threads=threads)
+    pb.run(TAU, FX, FY, 2, threads=threads)
     per_cell = (time.perf_counter() - t0) / (2 * n * probe_rows)
-    budget = 120.0
+    del pb
+    rows, budget = n, 120.0
     while rows > 1024 and per_cell * n * rows * (args.steps + warmup) > budget:
         rows //= 2
-    mask = np.zeros(n * rows, np.uint8)
-    mask[:n] = mask_full_row
-    mask[-n:] = mask_full_row
-    r = orc.s_to_r(n, rows, mask, orc.seeded_state(SEED, AMP, n, rows, mask, "f32"))
-    orc.pull_run(n, rows, mask, TAU, FX, FY, r, warmup, threads=threads)
+    mask = channel(rows)
+    bufs = orc.PullBuffers(n, rows, mask, orc.s_to_r(n, rows, mask, orc.seeded_state(SEED, AMP, n, rows, mask)))
+    bufs.run(TAU, FX, FY, warmup, threads=threads)
     t0 = time.perf_counter()
-    orc.pull_run(n, rows, mask, TAU, FX, FY, r, args.steps, threads=threads)
+    bufs.run(TAU, FX, FY, args.steps, threads=threads)
     dt = time.perf_counter() - t0
     value = n * rows * args.steps / dt / 1e6
     sample = (f"{n}x{rows} walled channel (full {n}x{n} rows bounded to fit ~2 min), "

@@ -18,13 +18,13 @@ static const REAL FN(W)[9] = {(REAL)4 / 9,  (REAL)1 / 9,  (REAL)1 / 9,  (REAL)1 
 
 /* Shifted equilibrium g_eq = w [drho + rho (3 cu + 4.5 cu cu - 1.5 usq)]
  * (src/common/d2q9.hpp:40-42). Evaluation order: ((3*cu) + ((4.5*cu)*cu)) - (1.5*usq). */
-static inline REAL FN(equilibrium_shifted)(REAL wi, REAL drho, REAL rho, REAL cu, REAL usq) {
+static inline __attribute__((always_inline)) REAL FN(equilibrium_shifted)(REAL wi, REAL drho, REAL rho, REAL cu, REAL usq) {
   return wi * (drho + rho * ((REAL)3 * cu + (REAL)4.5 * cu * cu - (REAL)1.5 * usq));
 }
 
 /* Guo source without its (1 - omega/2) prefactor (src/common/d2q9.hpp:46-50):
  * w [3 ((cx - ux) fx + (cy - uy) fy) + 9 (c.u)(c.F)]. */
-static inline REAL FN(guo_source)(REAL wi, REAL cxi, REAL cyi, REAL ux, REAL uy, REAL fx,
+static inline __attribute__((always_inline)) REAL FN(guo_source)(REAL wi, REAL cxi, REAL cyi, REAL ux, REAL uy, REAL fx,
                                   REAL fy) {
   const REAL cu = cxi * ux + cyi * uy;
   const REAL cf = cxi * fx + cyi * fy;
@@ -244,7 +244,7 @@ void FN(oracle_s_to_r)(int nx, int ny, const uint8_t* solid, int open_x, const R
 
 /* BGK + Guo collision of gathered populations gin, v0 operation order; writes 9 outputs with
  * stride n (SoA) starting at out. */
-static inline void FN(collide_store)(const REAL* gin, REAL omega, REAL force_prefactor, REAL fx,
+static inline __attribute__((always_inline)) void FN(collide_store)(const REAL* gin, REAL omega, REAL force_prefactor, REAL fx,
                                      REAL fy, REAL* out, size_t n) {
   REAL m0 = 0, mx = 0, my = 0;
 #pragma GCC unroll 9
@@ -268,10 +268,64 @@ static inline void FN(collide_store)(const REAL* gin, REAL omega, REAL force_pre
   }
 }
 
+/* Pull update of interior cell c (column x, 0 < x < nx - 1): both candidate loads are done
+ * unconditionally and selected by the source mask, and the collision is computed for solid
+ * cells too and stored as 0, so that the loop over x has no branch and vectorises (the
+ * structure of src/v1_omp/solver_v1.cpp:18-67). */
+static inline __attribute__((always_inline)) void FN(pull_cell)(
+    const REAL* restrict r, REAL* restrict rn, const uint8_t* restrict solid, size_t n,
+    const size_t* row, int x, REAL omega, REAL force_prefactor, REAL fx, REAL fy) {
+  const size_t c = row[1] + (size_t)x;
+  REAL gin[9];
+#pragma GCC unroll 9
+  for (int i = 0; i < 9; ++i) {
+    const size_t src = row[1 - CY[i]] + (size_t)(x - CX[i]);
+    const REAL streamed = r[i * n + src];
+    const REAL bounced = r[OPP[i] * n + c];
+    gin[i] = solid[src] ? bounced : streamed;
+  }
+  REAL m0 = 0, mx = 0, my = 0;
+#pragma GCC unroll 9
+  for (int i = 0; i < 9; ++i) {
+    m0 += gin[i];
+    mx += CX[i] * gin[i];
+    my += CY[i] * gin[i];
+  }
+  const REAL drho = m0;
+  const REAL rho = (REAL)1 + drho;
+  const REAL ux = (mx + (REAL)0.5 * fx) / rho;
+  const REAL uy = (my + (REAL)0.5 * fy) / rho;
+  const REAL usq = ux * ux + uy * uy;
+#pragma GCC unroll 9
+  for (int i = 0; i < 9; ++i) {
+    const REAL cu = CX[i] * ux + CY[i] * uy;
+    const REAL geq = FN(equilibrium_shifted)(FN(W)[i], drho, rho, cu, usq);
+    const REAL g_post = gin[i] - omega * (gin[i] - geq) +
+                        force_prefactor * FN(guo_source)(FN(W)[i], (REAL)CX[i], (REAL)CY[i], ux,
+                                                         uy, fx, fy);
+    rn[i * n + c] = solid[c] ? (REAL)0 : g_post;
+  }
+}
+
+/* Edge columns x = 0 and x = nx - 1: gather with the periodic wrap or the open-x rules. */
+static void FN(pull_edge)(const REAL* r, REAL* rn, const uint8_t* solid, int nx, int ny, int x,
+                          int y, int open_x, const REAL* eq_in, REAL omega, REAL force_prefactor,
+                          REAL fx, REAL fy) {
+  const size_t n = (size_t)nx * ny;
+  const size_t c = (size_t)y * nx + x;
+  REAL out[9] = {0};
+  if (!solid[c]) {
+    REAL gin[9];
+    FN(gather_pull)(r, solid, nx, ny, x, y, open_x, eq_in, gin);
+    FN(collide_store)(gin, omega, force_prefactor, fx, fy, out, 1);
+  }
+  for (int i = 0; i < 9; ++i) rn[i * n + c] = out[i];
+}
+
 /* One pull step on SoA post-collision states (r -> r_new), OpenMP over rows, restating the
  * structure of the reference's v1 solver (src/v1_omp/solver_v1.cpp:136-175): periodic rows
- * computed once per row, the two edge columns apart so that the interior loop has unit strides,
- * both candidate loads done unconditionally and selected by the source mask. Solid cells get 0. */
+ * computed once per row, the two edge columns apart so that the interior loop has unit strides
+ * and no branch. Solid cells get 0. */
 static void FN(pull_step)(int nx, int ny, const uint8_t* solid, REAL omega, REAL force_prefactor,
                           REAL fx, REAL fy, int open_x, const REAL* eq_in,
                           const REAL* restrict r, REAL* restrict rn) {
@@ -280,47 +334,26 @@ static void FN(pull_step)(int nx, int ny, const uint8_t* solid, REAL omega, REAL
   for (int y = 0; y < ny; ++y) {
     const size_t row[3] = {(size_t)(y == 0 ? ny - 1 : y - 1) * nx, (size_t)y * nx,
                            (size_t)(y == ny - 1 ? 0 : y + 1) * nx};
-    for (int x = 0; x < nx; ++x) {
-      const int edge = (x == 0 || x == nx - 1);
-      const size_t c = row[1] + x;
-      REAL gin[9];
-      if (edge) {
-        if (solid[c]) {
-          for (int i = 0; i < 9; ++i) rn[i * n + c] = 0;
-          continue;
-        }
-        FN(gather_pull)(r, solid, nx, ny, x, y, open_x, eq_in, gin);
-      } else {
-        /* interior column: neighbours x - 1 and x + 1 need no wrap */
-#pragma GCC unroll 9
-        for (int i = 0; i < 9; ++i) {
-          const size_t src = row[1 - CY[i]] + (size_t)(x - CX[i]);
-          const REAL streamed = r[i * n + src];
-          const REAL bounced = r[OPP[i] * n + c];
-          gin[i] = solid[src] ? bounced : streamed;
-        }
-      }
-      REAL out[9];
-      FN(collide_store)(gin, omega, force_prefactor, fx, fy, out, 1);
-      for (int i = 0; i < 9; ++i) rn[i * n + c] = solid[c] ? (REAL)0 : out[i];
-    }
+    FN(pull_edge)(r, rn, solid, nx, ny, 0, y, open_x, eq_in, omega, force_prefactor, fx, fy);
+#pragma GCC ivdep
+    for (int x = 1; x < nx - 1; ++x)
+      FN(pull_cell)(r, rn, solid, n, row, x, omega, force_prefactor, fx, fy);
+    if (nx > 1)
+      FN(pull_edge)(r, rn, solid, nx, ny, nx - 1, y, open_x, eq_in, omega, force_prefactor, fx,
+                    fy);
   }
 }
 
-/* Runs `steps` pull steps in place on the SoA state r with `threads` OpenMP threads (0: the
- * OpenMP default). Bitwise identical to oracle_v0_run on stream(r). Returns 0, -1 on
- * allocation failure. */
-int FN(oracle_pull_run)(int nx, int ny, const uint8_t* solid, REAL tau, REAL fx, REAL fy,
-                        int open_x, REAL u_in, REAL* r, int steps, int threads) {
-  const size_t n = (size_t)nx * ny * 9;
-  REAL* rn = (REAL*)malloc(n * sizeof(REAL));
-  if (!rn) return -1;
+/* Runs `steps` pull steps ping-ponging between caller-provided SoA buffers r (input) and rn
+ * (scratch, same size), with `threads` OpenMP threads (0: the OpenMP default). Returns 0 when
+ * the result is in r, 1 when it is in rn. Bitwise identical to oracle_v0_run on stream(r). */
+int FN(oracle_pull_steps)(int nx, int ny, const uint8_t* solid, REAL tau, REAL fx, REAL fy,
+                          int open_x, REAL u_in, REAL* r, REAL* rn, int steps, int threads) {
 #ifdef _OPENMP
   if (threads > 0) omp_set_num_threads(threads);
 #else
   (void)threads;
 #endif
-  memset(rn, 0, n * sizeof(REAL));
   const REAL omega = (REAL)1 / tau;
   const REAL force_prefactor = (REAL)1 - (REAL)0.5 * omega;
   REAL eq_in[9] = {0};
@@ -333,7 +366,27 @@ int FN(oracle_pull_run)(int nx, int ny, const uint8_t* solid, REAL tau, REAL fx,
     a = b;
     b = t;
   }
-  if (a != r) memcpy(r, a, n * sizeof(REAL));
+  return a == r ? 0 : 1;
+}
+
+/* Zero-fills an SoA buffer with the row distribution of pull_step (first touch). */
+void FN(oracle_first_touch)(int nx, int ny, REAL* r) {
+  const size_t n = (size_t)nx * ny;
+#pragma omp parallel for schedule(static)
+  for (int y = 0; y < ny; ++y)
+    for (int i = 0; i < 9; ++i) memset(&r[i * n + (size_t)y * nx], 0, (size_t)nx * sizeof(REAL));
+}
+
+/* Runs `steps` pull steps in place on the SoA state r (allocates the second buffer). Returns 0,
+ * -1 on allocation failure. */
+int FN(oracle_pull_run)(int nx, int ny, const uint8_t* solid, REAL tau, REAL fx, REAL fy,
+                        int open_x, REAL u_in, REAL* r, int steps, int threads) {
+  const size_t n = (size_t)nx * ny * 9;
+  REAL* rn = (REAL*)malloc(n * sizeof(REAL));
+  if (!rn) return -1;
+  FN(oracle_first_touch)(nx, ny, rn);
+  if (FN(oracle_pull_steps)(nx, ny, solid, tau, fx, fy, open_x, u_in, r, rn, steps, threads))
+    memcpy(r, rn, n * sizeof(REAL));
   free(rn);
   return 0;
 }

@@ -74,6 +74,10 @@ class _Lib:
             fn("oracle_pull_run").restype = C.c_int
             fn("oracle_pull_run").argtypes = [C.c_int, C.c_int, _u8p, t, t, t, C.c_int, t, p,
                                               C.c_int, C.c_int]
+            fn("oracle_pull_steps").restype = C.c_int
+            fn("oracle_pull_steps").argtypes = [C.c_int, C.c_int, _u8p, t, t, t, C.c_int, t, p, p,
+                                                C.c_int, C.c_int]
+            fn("oracle_first_touch").argtypes = [C.c_int, C.c_int, p]
             fn("oracle_seeded_state").argtypes = [C.c_uint64, C.c_double, C.c_int, C.c_int,
                                                   _u8p, p]
 
@@ -142,6 +146,27 @@ def pull_run(nx, ny, solid, tau, fx, fy, r, steps, open_x=False, u_in=0.0, real=
     if rc != 0:
         raise MemoryError("oracle_pull_run: allocation failed")
     return r
+
+
+class PullBuffers:
+    """Two SoA buffers for timed pull runs (no allocation inside the timed region)."""
+
+    def __init__(self, nx, ny, solid, r0, real="f32"):
+        self.nx, self.ny, self.real = nx, ny, real
+        self.solid = _mask(solid)
+        self.a = np.empty(nx * ny * 9, _dtype(real))
+        self.b = np.empty_like(self.a)
+        _f("oracle_first_touch", real)(nx, ny, self.a)
+        _f("oracle_first_touch", real)(nx, ny, self.b)
+        self.a[:] = r0
+
+    def run(self, tau, fx, fy, steps, open_x=False, u_in=0.0, threads=0):
+        which = _f("oracle_pull_steps", self.real)(self.nx, self.ny, self.solid, tau, fx, fy,
+                                                   int(open_x), u_in, self.a, self.b, steps,
+                                                   threads)
+        if which:
+            self.a, self.b = self.b, self.a
+        return self.a
 
 
 def s_to_r(nx, ny, solid, s, open_x=False, real="f32") -> np.ndarray:
