@@ -141,6 +141,34 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * pitch in elements, and the current read buffer. */
 int lbm_state_view(lbm_solver* s, void** current, long long* plane_stride, int* row_pitch);
 
+/* Largest ny accepted by lbm_total_mass_noalloc (rows of its static scratch). */
+#define LBM_NOALLOC_MAX_ROWS 16384
+
+/* Total mass of a pull state held in caller memory, without allocating any device memory.
+ * No counterpart in the reference: it is an extra entry point for callers that cannot let a
+ * library call cudaMalloc/cudaFree, such as hosts that own all device memory through their own
+ * pool or arena, or loops that cannot afford the device synchronisation those calls may cause.
+ * The reduction's scratch lives in static device arrays of the library (one FP64 partial and
+ * one count per row, 256 KiB, held by every GPU that loads the library until the process
+ * exits); nothing else is used.
+ *   planes        device pointer to a pull state: 9 planes, plane i row y column x at
+ *                 planes[i*plane_stride + y*row_pitch + x] (e.g. lbm_state_view's pointer);
+ *   precision     LBM_FP32 (float elements) or LBM_FP64 (double);
+ *   solid         device pointer to nx*ny bytes, row-major, non-zero = solid cell;
+ *   mass          device pointer to one double that receives fluid-cell count + the sum of the
+ *                 stored populations of the fluid cells (the total mass of a periodic domain:
+ *                 streaming only permutes the fluid slots);
+ *   stream        cudaStream_t the two kernels are enqueued on (asynchronous; 0 = legacy);
+ *   err, err_size optional buffer for a message (may be null).
+ * Returns LBM_ERR_INVALID_ARG for null pointers, bad sizes, or ny > LBM_NOALLOC_MAX_ROWS;
+ * LBM_ERR_UNSUPPORTED for the 16-bit forms. The first call on a device looks up the device
+ * address of the scratch (cudaGetSymbolAddress), so make that first call before any stream
+ * capture. All calls share the same scratch and every call rewrites the rows it reads: calls
+ * that overlap on the GPU (e.g. on two streams) race and must be serialised by the caller. */
+int lbm_total_mass_noalloc(const void* planes, int precision, int nx, int ny, int row_pitch,
+                           long long plane_stride, const uint8_t* solid, double* mass,
+                           void* stream, char* err, size_t err_size);
+
 #ifdef __cplusplus
 }
 #endif
