@@ -40,7 +40,8 @@ enum {
   LBM_ERR_CUDA = 2,        /* a CUDA runtime error (the reference aborts, cuda_check.hpp:17-27) */
   LBM_ERR_OUT_OF_MEMORY = 3,
   LBM_ERR_DIVERGED = 4, /* non-finite density (the reference's driver throws, driver.hpp:217-218) */
-  LBM_ERR_UNSUPPORTED = 5
+  LBM_ERR_UNSUPPORTED = 5,
+  LBM_ERR_TIMEOUT = 6 /* a kernel's bounded wait ran out (reported by the next synchronising call) */
 };
 
 /* Storage / arithmetic forms. FP32 and FP64 are bit-exact with the reference's v0 in float and
@@ -137,9 +138,89 @@ int lbm_get_shape(const lbm_solver* s, int* nx, int* ny, int* precision);
  * grid of resident blocks). Used by the autotuner. */
 int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
 
+/* Step kernel variant (results are identical; used by the autotuner): 0 and 2 load a chunk's
+ * plane vectors when the warp reaches it, 1 and 3 also load the warp's next chunk while the
+ * current one is computed (more bytes in flight, more registers); 2 and 3 cap the registers for
+ * 4 and 3 resident blocks per SM. 4, 5, 6: warp-specialised kernel, a producer warp streams
+ * tiles into a shared-memory ring of 2, 3, 4 stages with bulk asynchronous copies (TMA) and
+ * eight consumer warps collide from shared memory. -1 (the default): 4 for grids whose rows hold
+ * whole tiles and enough tiles to fill the GPU, 0 otherwise. */
+int lbm_set_variant(lbm_solver* s, int variant);
+
 /* Device memory of the two population buffers (for zero-copy consumers): plane stride and row
  * pitch in elements, and the current read buffer. */
 int lbm_state_view(lbm_solver* s, void** current, long long* plane_stride, int* row_pitch);
+
+/* ---------------------------------------------------------------------------------------------
+ * Adjoint (no counterpart in the reference): gradients of a flow objective with respect to the
+ * body force, tau and a per-cell Brinkman drag field alpha, as a forward/backward pair.
+ *   Forward model: the reference's step with a drag force F_tot = F - alpha rho u, the Guo
+ *   velocity u = (m + F/2) / (rho (1 + alpha/2)); alpha = 0 is the plain method, bit for bit.
+ *   Objective: J = mean over the last `window` states (t = steps - window + 1 .. steps) of the
+ *   mean u_x over fluid cells.
+ *   The forward run stores the state every `checkpoint_every` steps; the backward run recomputes
+ *   each segment from its checkpoint and runs the adjoint step (transposed pull gather with
+ *   transposed bounce-back, collision Jacobian transposed) backwards through it. Parameter
+ *   gradients are accumulated in double. Closed (periodic in x and y) domains only.
+ *   A batch of instances shares geometry, tau and force; each has its own alpha field.
+ * ------------------------------------------------------------------------------------------- */
+typedef struct lbm_adjoint lbm_adjoint;
+
+/* precision: LBM_FP32 or LBM_FP64; batch >= 1 instances; checkpoint_every >= 1. */
+int lbm_adj_create(int nx, int ny, const uint8_t* solid, double tau, double fx, double fy,
+                   int precision, int batch, int checkpoint_every, lbm_adjoint** out);
+int lbm_adj_destroy(lbm_adjoint* a);
+const char* lbm_adj_last_error(const lbm_adjoint* a);
+/* New tau / force for all instances (e.g. for finite differences). */
+int lbm_adj_set_params(lbm_adjoint* a, double tau, double fx, double fy);
+/* alpha: batch * nx * ny doubles (instance-major, row-major), or null for alpha = 0. */
+int lbm_adj_set_alpha(lbm_adjoint* a, const double* alpha);
+/* Runs `steps` steps from s0 (batch * nx * ny * 9 values of the host type in v0 layout, or null
+ * for the rest state f_i - w_i = 0), storing checkpoints; J receives `batch` objectives. */
+int lbm_adj_forward(lbm_adjoint* a, const void* s0, int steps, int window, double* J);
+/* Gradients of J for every instance (arrays of `batch` values; dalpha: batch * nx * ny, any
+ * pointer may be null). Needs a preceding lbm_adj_forward. */
+int lbm_adj_backward(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* dalpha);
+/* Post-streaming populations (v0 layout) of one instance after the forward run. */
+int lbm_adj_get_populations(lbm_adjoint* a, int instance, void* s_host);
+/* Average device time of one forward step and of one backward step (recomputation included)
+ * of the last runs, in seconds. */
+int lbm_adj_step_times(lbm_adjoint* a, double* forward_step_s, double* backward_step_s);
+
+/* ---------------------------------------------------------------------------------------------
+ * Batched ensemble (no counterpart in the reference): `count` independent closed channels of
+ * uneven sizes, each with its own mask, tau and force, stepped together by one persistent kernel
+ * launch per time step, replayed from a CUDA graph. Same arithmetic as the single-grid solver
+ * (FP32 / FP64 bit-exact with the reference's v0 per instance).
+ * ------------------------------------------------------------------------------------------- */
+typedef struct lbm_batch lbm_batch;
+
+/* solid[k]: nx[k]*ny[k] bytes; count <= 4096. */
+int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* const* solid,
+                     const double* tau, const double* fx, const double* fy, int precision,
+                     lbm_batch** out);
+int lbm_batch_destroy(lbm_batch* b);
+const char* lbm_batch_last_error(const lbm_batch* b);
+/* Every instance at the equilibrium of (rho0, ux0, uy0). */
+int lbm_batch_init_equilibrium(lbm_batch* b, double rho0, double ux0, double uy0);
+/* Post-streaming state of one instance, v0 layout, host type (as lbm_set_populations). */
+int lbm_batch_set_populations(lbm_batch* b, int instance, const void* s_host);
+int lbm_batch_get_populations(lbm_batch* b, int instance, void* s_host);
+int lbm_batch_total_mass(lbm_batch* b, int instance, double* mass);
+/* `steps` steps of every instance (one launch per step, graph-replayed), then waits. */
+int lbm_batch_run(lbm_batch* b, int steps);
+/* Same, timed with CUDA events on the batch's stream (seconds). */
+int lbm_batch_timed_run(lbm_batch* b, int steps, double* seconds);
+/* The comparison point: the same steps with one launch per instance per step. */
+int lbm_batch_run_separate(lbm_batch* b, int steps, double* seconds);
+/* Launch shape: cells per thread (the two vector widths of the form, 0 = widest), threads per
+ * block (multiple of 32, <= 256), blocks (0 = all resident blocks). */
+int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, int grid_blocks);
+/* Times the candidate launch shapes on the current ensemble and keeps the fastest; with a cache
+ * path the choice is read from / appended to that file (one line per GPU, form and size). The
+ * state is restored afterwards. report (may be null) receives a one-line summary. */
+int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_t report_size);
+int lbm_batch_info(const lbm_batch* b, int* count, long long* total_cells, int* items);
 
 /* Largest ny accepted by lbm_total_mass_noalloc (rows of its static scratch). */
 #define LBM_NOALLOC_MAX_ROWS 16384

@@ -116,7 +116,12 @@ class SolverB200 {
   std::size_t cells() const { return static_cast<std::size_t>(nx_) * static_cast<std::size_t>(ny_); }
   void check(int rc, const char* what) const {
     if (rc == LBM_OK) return;
-    const std::string msg = std::string(what) + ": " + (h_ ? lbm_last_error(h_) : "");
+    static const char* const names[] = {"ok", "invalid argument", "CUDA error", "out of memory",
+                                        "diverged", "unsupported", "timeout"};
+    const std::string detail = h_ ? lbm_last_error(h_) : "";
+    const std::string msg = std::string(what) + ": " +
+                            (rc >= 0 && rc <= 6 ? names[rc] : "error") +
+                            (detail.empty() ? "" : " (" + detail + ")");
     if (rc == LBM_ERR_INVALID_ARG) throw std::invalid_argument(msg);
     throw std::runtime_error(msg);
   }

@@ -7,7 +7,7 @@ populations / populations_at / threads / bench_info / nx / ny / solid. Errors fo
 reference: invalid arguments raise ValueError (std::invalid_argument there), CUDA failures raise
 RuntimeError (the reference aborts).
 
-The binding loads lib/liblbm_b200.so (built by build.py). There is no CPU fallback: without
+The binding loads lib/liblbm_b200.so (built by buildlib.py). There is no CPU fallback: without
 the library, or without a GPU, constructing a Solver raises.
 """
 from __future__ import annotations
@@ -17,7 +17,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import geometry  # noqa: F401  (re-exported)
+from . import geometry, workloads  # noqa: F401  (re-exported)
 from .geometry import make_channel, make_cylinder, poiseuille_force  # noqa: F401
 
 _HERE = Path(__file__).resolve().parent
@@ -28,15 +28,15 @@ PRECISIONS = {"fp32": FP32, "fp64": FP64, "fp16": FP16_STORE, "fp16_store": FP16
               "bf16": BF16_STORE, "bf16_store": BF16_STORE}
 HOST_DTYPE = {FP32: np.float32, FP64: np.float64, FP16_STORE: np.float32, BF16_STORE: np.float32}
 
-OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_DIVERGED, ERR_UNSUPPORTED = range(6)
+OK, ERR_INVALID_ARG, ERR_CUDA, ERR_OUT_OF_MEMORY, ERR_DIVERGED, ERR_UNSUPPORTED, ERR_TIMEOUT = range(7)
 
 _lib = None
 
 
 def build(**kw) -> Path:
-    """Compiles the CUDA library (see build.py)."""
+    """Compiles the CUDA library (see buildlib.py)."""
     import importlib
-    return importlib.import_module(f"{__name__}.build").build(**kw)
+    return importlib.import_module(f"{__name__}.buildlib").build(**kw)
 
 
 def lib() -> C.CDLL:
@@ -68,7 +68,30 @@ def lib() -> C.CDLL:
             "lbm_device_info": ([vp, C.c_char_p, C.c_size_t], i),
             "lbm_get_shape": ([vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)], i),
             "lbm_set_launch": ([vp, i, i], i),
+            "lbm_set_variant": ([vp, i], i),
             "lbm_state_view": ([vp, C.POINTER(vp), C.POINTER(C.c_longlong), C.POINTER(i)], i),
+            "lbm_adj_create": ([i, i, vp, d, d, d, i, i, i, C.POINTER(vp)], i),
+            "lbm_adj_destroy": ([vp], i),
+            "lbm_adj_last_error": ([vp], C.c_char_p),
+            "lbm_adj_set_params": ([vp, d, d, d], i),
+            "lbm_adj_set_alpha": ([vp, vp], i),
+            "lbm_adj_forward": ([vp, vp, i, i, vp], i),
+            "lbm_adj_backward": ([vp, vp, vp, vp, vp], i),
+            "lbm_adj_get_populations": ([vp, i, vp], i),
+            "lbm_adj_step_times": ([vp, C.POINTER(d), C.POINTER(d)], i),
+            "lbm_batch_create": ([i, vp, vp, vp, vp, vp, vp, i, C.POINTER(vp)], i),
+            "lbm_batch_destroy": ([vp], i),
+            "lbm_batch_last_error": ([vp], C.c_char_p),
+            "lbm_batch_init_equilibrium": ([vp, d, d, d], i),
+            "lbm_batch_set_populations": ([vp, i, vp], i),
+            "lbm_batch_get_populations": ([vp, i, vp], i),
+            "lbm_batch_total_mass": ([vp, i, C.POINTER(d)], i),
+            "lbm_batch_run": ([vp, i], i),
+            "lbm_batch_timed_run": ([vp, i, C.POINTER(d)], i),
+            "lbm_batch_run_separate": ([vp, i, C.POINTER(d)], i),
+            "lbm_batch_set_launch": ([vp, i, i, i], i),
+            "lbm_batch_autotune": ([vp, C.c_char_p, C.c_char_p, C.c_size_t], i),
+            "lbm_batch_info": ([vp, C.POINTER(i), C.POINTER(C.c_longlong), C.POINTER(i)], i),
         }
         for name, (args, res) in sig.items():
             f = getattr(L, name)
@@ -208,6 +231,9 @@ class Solver:
     def set_launch(self, block_threads: int, grid_blocks: int = 0):
         self._check(lib().lbm_set_launch(self._h, block_threads, grid_blocks))
 
+    def set_variant(self, variant: int):
+        self._check(lib().lbm_set_variant(self._h, variant))
+
     def set_stream(self, stream_handle: int):
         self._check(lib().lbm_set_stream(self._h, C.c_void_p(stream_handle)))
 
@@ -219,6 +245,183 @@ class Solver:
 
     def solid(self) -> np.ndarray:
         return self._solid
+
+
+class Adjoint:
+    """Forward/backward pair of the adjoint (C ABI lbm_adj_*): gradients of
+    J = mean over the last `window` states of the mean u_x over fluid cells, with respect to tau,
+    the body force and a per-cell Brinkman drag field alpha (F_tot = F - alpha rho u). A batch of
+    instances shares geometry, tau and force and has one alpha field each. Closed domains."""
+
+    def __init__(self, nx, ny, tau, fx, fy, solid, precision="fp64", batch=1,
+                 checkpoint_every=100):
+        self.nx, self.ny, self.batch = int(nx), int(ny), int(batch)
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.dtype = HOST_DTYPE[self.precision]
+        self._solid = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+        self._h = C.c_void_p()
+        rc = lib().lbm_adj_create(self.nx, self.ny, _ptr(self._solid), tau, fx, fy, self.precision,
+                                  self.batch, checkpoint_every, C.byref(self._h))
+        if rc != OK:
+            _raise(rc, "lbm_adj_create failed")
+
+    def _check(self, rc):
+        if rc != OK:
+            _raise(rc, (lib().lbm_adj_last_error(self._h) or b"").decode())
+
+    def close(self):
+        if self._h:
+            lib().lbm_adj_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def set_params(self, tau, fx, fy):
+        self._check(lib().lbm_adj_set_params(self._h, tau, fx, fy))
+
+    def set_alpha(self, alpha):
+        """alpha: (batch, nx*ny) or (nx*ny,) for batch 1, or None for alpha = 0."""
+        if alpha is None:
+            self._check(lib().lbm_adj_set_alpha(self._h, None))
+            return
+        self._alpha = np.ascontiguousarray(alpha, dtype=np.float64).reshape(-1)
+        if self._alpha.size != self.batch * self.nx * self.ny:
+            raise ValueError("alpha must hold batch * nx * ny values")
+        self._check(lib().lbm_adj_set_alpha(self._h, _ptr(self._alpha)))
+
+    def forward(self, steps, window, s0=None) -> np.ndarray:
+        J = np.zeros(self.batch, np.float64)
+        if s0 is not None:
+            s0 = np.ascontiguousarray(s0, dtype=self.dtype).reshape(-1)
+            if s0.size != self.batch * self.nx * self.ny * 9:
+                raise ValueError("s0 must hold batch * nx * ny * 9 values")
+        self._check(lib().lbm_adj_forward(self._h, None if s0 is None else _ptr(s0), steps,
+                                          window, _ptr(J)))
+        return J
+
+    def backward(self, want_alpha=True):
+        """Returns dict(tau, fx, fy: arrays of batch values, alpha: (batch, nx*ny) or None)."""
+        b = self.batch
+        dt, dfx, dfy = (np.zeros(b) for _ in range(3))
+        da = np.zeros(b * self.nx * self.ny) if want_alpha else None
+        self._check(lib().lbm_adj_backward(self._h, _ptr(dt), _ptr(dfx), _ptr(dfy),
+                                           None if da is None else _ptr(da)))
+        return {"tau": dt, "fx": dfx, "fy": dfy,
+                "alpha": None if da is None else da.reshape(b, -1)}
+
+    def populations(self, instance=0) -> np.ndarray:
+        out = np.empty(self.nx * self.ny * 9, self.dtype)
+        self._check(lib().lbm_adj_get_populations(self._h, instance, _ptr(out)))
+        return out
+
+    def step_times(self):
+        f, b = C.c_double(), C.c_double()
+        self._check(lib().lbm_adj_step_times(self._h, C.byref(f), C.byref(b)))
+        return f.value, b.value
+
+
+class Batch:
+    """Ensemble of independent closed channels of uneven sizes stepped by one persistent launch
+    per time step (C ABI lbm_batch_*). specs: list of dict(nx, ny, mask, tau, fx[, fy])."""
+
+    def __init__(self, specs, precision="fp32"):
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.dtype = HOST_DTYPE[self.precision]
+        self.specs = specs
+        n = len(specs)
+        self._nx = np.array([s["nx"] for s in specs], np.int32)
+        self._ny = np.array([s["ny"] for s in specs], np.int32)
+        self._masks = [np.ascontiguousarray(s["mask"], np.uint8).reshape(-1) for s in specs]
+        ptrs = (C.c_void_p * n)(*[m.ctypes.data for m in self._masks])
+        self._tau = np.array([s["tau"] for s in specs], np.float64)
+        self._fx = np.array([s["fx"] for s in specs], np.float64)
+        self._fy = np.array([s.get("fy", 0.0) for s in specs], np.float64)
+        self._h = C.c_void_p()
+        rc = lib().lbm_batch_create(n, _ptr(self._nx), _ptr(self._ny), C.cast(ptrs, C.c_void_p),
+                                    _ptr(self._tau), _ptr(self._fx), _ptr(self._fy),
+                                    self.precision, C.byref(self._h))
+        if rc != OK:
+            _raise(rc, "lbm_batch_create failed")
+
+    def _check(self, rc):
+        if rc != OK:
+            _raise(rc, (lib().lbm_batch_last_error(self._h) or b"").decode())
+
+    def close(self):
+        if self._h:
+            lib().lbm_batch_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __len__(self):
+        return len(self.specs)
+
+    def init_equilibrium(self, rho0, ux0, uy0):
+        self._check(lib().lbm_batch_init_equilibrium(self._h, rho0, ux0, uy0))
+
+    def set_populations(self, k, s):
+        s = np.ascontiguousarray(s, dtype=self.dtype).reshape(-1)
+        if s.size != int(self._nx[k]) * int(self._ny[k]) * 9:
+            raise ValueError("populations must hold nx*ny*9 values")
+        self._check(lib().lbm_batch_set_populations(self._h, k, _ptr(s)))
+
+    def populations(self, k) -> np.ndarray:
+        out = np.empty(int(self._nx[k]) * int(self._ny[k]) * 9, self.dtype)
+        self._check(lib().lbm_batch_get_populations(self._h, k, _ptr(out)))
+        return out
+
+    def total_mass(self, k) -> float:
+        m = C.c_double()
+        self._check(lib().lbm_batch_total_mass(self._h, k, C.byref(m)))
+        return m.value
+
+    def run(self, steps):
+        self._check(lib().lbm_batch_run(self._h, steps))
+
+    def timed_run(self, steps) -> float:
+        t = C.c_double()
+        self._check(lib().lbm_batch_timed_run(self._h, steps, C.byref(t)))
+        return t.value
+
+    def run_separate(self, steps) -> float:
+        t = C.c_double()
+        self._check(lib().lbm_batch_run_separate(self._h, steps, C.byref(t)))
+        return t.value
+
+    def set_launch(self, cells_per_thread=0, block_threads=256, grid_blocks=0):
+        self._check(lib().lbm_batch_set_launch(self._h, cells_per_thread, block_threads, grid_blocks))
+
+    def autotune(self, cache_path=None) -> str:
+        buf = C.create_string_buffer(4096)
+        self._check(lib().lbm_batch_autotune(self._h, None if cache_path is None else str(cache_path).encode(),
+                                             buf, 4096))
+        return buf.value.decode()
+
+    def info(self):
+        n, cells, items = C.c_int(), C.c_longlong(), C.c_int()
+        self._check(lib().lbm_batch_info(self._h, C.byref(n), C.byref(cells), C.byref(items)))
+        return {"count": n.value, "cells": cells.value, "chunks": items.value}
 
 
 def version() -> str:

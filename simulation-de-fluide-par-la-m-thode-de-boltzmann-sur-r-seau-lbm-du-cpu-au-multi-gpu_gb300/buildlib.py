@@ -32,9 +32,15 @@ def nvcc() -> str:
     raise FileNotFoundError("nvcc not found")
 
 
-def common_flags() -> list[str]:
+# Translation units whose plain-operator arithmetic may be contracted into FMA: their exact
+# parts use explicit round-to-nearest intrinsics, which are never contracted.
+FMAD_TRUE = {"adjoint.cu"}
+
+
+def common_flags(src: Path | None = None) -> list[str]:
+    fmad = "--fmad=true" if src is not None and src.name in FMAD_TRUE else "--fmad=false"
     return ARCH + [
-        "-O3", "-std=c++17", "-lineinfo", "--fmad=false", "-Xcompiler", "-fPIC",
+        "-O3", "-std=c++17", "-lineinfo", fmad, "-Xcompiler", "-fPIC",
         "-Xcompiler", "-ffp-contract=off", "-I", str(CSRC), "-I", str(ROOT / "include"),
     ]
 
@@ -43,12 +49,28 @@ def sources() -> list[Path]:
     return sorted(CSRC.glob("*.cu"))
 
 
+DRIVER = PKG / "driver" / "lbm_b200_main.cpp"
+EXES = {"lbm_b200": [], "lbm_b200_double": ["-DLBM_REAL_DOUBLE"]}
+
+
 def _stale(objs: list[Path]) -> bool:
-    if not LIB.exists():
+    if not LIB.exists() or any(not (OUT_DIR / e).exists() for e in EXES):
         return True
-    t = LIB.stat().st_mtime
-    deps = list(CSRC.glob("*")) + [ROOT / "include" / "lbm_b200.h", Path(__file__)]
+    t = min([LIB.stat().st_mtime] + [(OUT_DIR / e).stat().st_mtime for e in EXES])
+    deps = list(CSRC.glob("*")) + list((ROOT / "include").glob("*")) + [DRIVER, Path(__file__)]
     return any(p.stat().st_mtime > t for p in deps if p.exists())
+
+
+def build_driver() -> None:
+    """The command-line driver (float and double builds), linked against the library."""
+    cxx = os.environ.get("CXX", "g++")
+    for exe, defs in EXES.items():
+        cmd = [cxx, "-std=c++17", "-O2", "-ffp-contract=off", *defs, "-I", str(ROOT / "include"),
+               str(DRIVER), "-L", str(OUT_DIR), "-llbm_b200", "-Wl,-rpath,$ORIGIN",
+               "-o", str(OUT_DIR / exe)]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError(f"driver build failed:\n{r.stderr}")
 
 
 def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) -> Path:
@@ -60,7 +82,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     extra = ["-Xptxas", "-v"] if ptxas_info else []
 
     def compile_one(src: Path, obj: Path):
-        cmd = [cc, *common_flags(), *extra, "-c", str(src), "-o", str(obj)]
+        cmd = [cc, *common_flags(src), *extra, "-c", str(src), "-o", str(obj)]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             raise RuntimeError(f"nvcc failed on {src.name}:\n{r.stdout}\n{r.stderr}")
@@ -77,6 +99,7 @@ def build(verbose: bool = False, ptxas_info: bool = False, force: bool = False) 
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, LIB)
+    build_driver()
     return LIB
 
 

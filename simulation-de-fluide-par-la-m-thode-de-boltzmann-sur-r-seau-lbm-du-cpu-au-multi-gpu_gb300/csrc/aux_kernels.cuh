@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kReduceThreads)
 }
 
 // Second pass: one block adds the partials in a fixed order; out[0] = fluid_cells + sum.
-__global__ void __launch_bounds__(kReduceThreads)
+static __global__ void __launch_bounds__(kReduceThreads)
     mass_final_kernel(const double* __restrict__ partials, int count, double fluid_cells,
                       double* __restrict__ out) {
   __shared__ double smem[32];

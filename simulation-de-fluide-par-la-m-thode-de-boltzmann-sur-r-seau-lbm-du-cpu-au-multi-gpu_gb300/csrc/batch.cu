@@ -1,0 +1,710 @@
+// Batched ensemble: many independent channels of uneven sizes stepped by one persistent launch.
+//
+// All instances live in one allocation per state buffer (each instance's 9 planes at a
+// 128-byte-aligned offset) and one mask allocation. A device table describes every instance
+// (offsets, geometry, collision constants, first global chunk index). The step kernel's warps
+// walk the global chunk list (chunks of 32 * G cells of one row of one instance), find their
+// instance by binary search over the first-chunk indices staged in shared memory, and run the
+// same chunk code as the single-grid kernel (step_kernel.cuh). Steps are replayed from a CUDA
+// graph of kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
+// instance per step (the comparison point). lbm_batch_autotune() times the candidate launch
+// shapes (cells per thread G, i.e. the chunk width 32 G, threads per block, blocks per SM) on the
+// actual ensemble and keeps the fastest, caching the choice per GPU, form and ensemble size.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <new>
+#include <sstream>
+#include <string>
+#include <vector>
+
+#include "aux_kernels.cuh"
+#include "lbm_b200.h"
+#include "solver_internal.h"
+#include "step_kernel.cuh"
+
+using namespace lbm_b200;
+
+namespace {
+
+constexpr int kBatchThreads = 256;
+constexpr int kBatchMaxInstances = 4096;  // first-chunk indices staged in shared memory
+constexpr int kGraphSteps = 64;
+
+template <class Consts>
+struct BatchInst {
+  long long off;       // element offset of the instance's planes in a state buffer
+  long long mask_off;  // word offset of its mask rows
+  Grid2D g;
+  int cpr;     // chunks per row for the launch's G
+  int item0;   // first global chunk index
+  Consts k;
+};
+
+template <class ST, class Phys>
+struct BatchArgs {
+  const ST* src;
+  ST* dst;
+  const uint32_t* mask;
+  const BatchInst<typename Phys::Consts>* inst;
+  int count;
+  int items;
+  PlaneScales sc;
+};
+
+template <class ST, class Phys, int G>
+__global__ void __launch_bounds__(kBatchThreads)
+    batch_step_kernel(const BatchArgs<ST, Phys> a) {
+  using T = typename StoreTraits<ST>::T;
+  __shared__ int s_item0[kBatchMaxInstances];
+  for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_item0[k] = a.inst[k].item0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < a.items; item += nwarps) {
+    int lo = 0, hi = a.count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_item0[mid] <= item)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const BatchInst<typename Phys::Consts>& d = a.inst[lo];
+    StepArgs<ST, Phys> p;
+    p.src = a.src + d.off;
+    p.dst = a.dst + d.off;
+    p.mask = a.mask + d.mask_off;
+    p.g = d.g;
+    p.cpr = d.cpr;
+    p.items = d.cpr * d.g.ny;
+    p.k = d.k;
+    p.sc = a.sc;
+    const Chunk c = chunk_at<G>(item - d.item0, d.cpr, d.g.nx, d.g.ny, lane);
+    T v[kQ][G];
+    load_planes<ST, Phys, G>(p, c, v);
+    process_chunk<ST, Phys, false, G>(p, c, v, lane);
+  }
+}
+
+template <class ST>
+struct BForm;
+template <>
+struct BForm<float> {
+  using Phys = ExactPhys<ExactF32>;
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_collide_consts<float>(float(tau), float(fx), float(fy));
+  }
+};
+template <>
+struct BForm<double> {
+  using Phys = ExactPhys<ExactF64>;
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_collide_consts<double>(tau, fx, fy);
+  }
+};
+template <>
+struct BForm<__half> {
+  using Phys = FastPhys;
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_fast_consts(float(tau), float(fx), float(fy));
+  }
+};
+template <>
+struct BForm<__nv_bfloat16> {
+  using Phys = FastPhys;
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_fast_consts(float(tau), float(fx), float(fy));
+  }
+};
+
+}  // namespace
+
+struct lbm_batch {
+  int precision = LBM_FP32, elem = 4, vec = 4, host_elem = 4, count = 0;
+  struct Inst {
+    int nx, ny;
+    double tau, fx, fy;
+    long long off, mask_off, fluid;
+    Grid2D g;
+  };
+  std::vector<Inst> inst;
+  long long total_elems = 0, total_cells = 0;
+  void* buf[2] = {nullptr, nullptr};
+  int cur = 0;
+  uint32_t* mask_d = nullptr;
+  void* table_d = nullptr;  // BatchInst<Consts>[count] for the current G
+  int table_G = 0;
+  void* stage = nullptr;
+  size_t stage_bytes = 0;
+  double* red = nullptr;
+  int red_blocks = 0;
+  PlaneScales sc{};
+  // launch configuration (autotuned)
+  int G = 0, block = kBatchThreads, grid = 0, items = 0, grid_eff = 1;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaGraphExec_t graph = nullptr;
+  int graph_cur = -1;  // buffer parity the graph was captured from
+  int sm_count = 0, device = 0;
+  std::string err, tune_report;
+};
+
+namespace {
+
+int bfail(lbm_batch* b, int code, const std::string& msg) {
+  if (b) b->err = msg;
+  return code;
+}
+
+#define B_CUDA(b, call)                                                                          \
+  do {                                                                                           \
+    const cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess) {                                                                     \
+      cudaGetLastError();                                                                        \
+      return bfail(b, e_ == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA,    \
+                   std::string(#call) + ": " + cudaGetErrorString(e_));                          \
+    }                                                                                            \
+  } while (0)
+
+void drop_graph(lbm_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  b->graph = nullptr;
+  b->graph_cur = -1;
+}
+
+// Builds the device instance table for cells-per-thread G.
+template <class ST>
+int build_table(lbm_batch* b, int G) {
+  using Consts = typename BForm<ST>::Phys::Consts;
+  std::vector<BatchInst<Consts>> tab(b->count);
+  int item = 0;
+  for (int k = 0; k < b->count; ++k) {
+    const auto& in = b->inst[k];
+    BatchInst<Consts>& d = tab[k];
+    d.off = in.off;
+    d.mask_off = in.mask_off;
+    d.g = in.g;
+    d.cpr = (in.nx + 32 * G - 1) / (32 * G);
+    d.item0 = item;
+    d.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
+    item += d.cpr * in.ny;
+  }
+  if (!b->table_d) B_CUDA(b, cudaMalloc(&b->table_d, b->count * sizeof(BatchInst<Consts>)));
+  B_CUDA(b, cudaMemcpy(b->table_d, tab.data(), b->count * sizeof(BatchInst<Consts>), cudaMemcpyHostToDevice));
+  b->items = item;
+  b->table_G = G;
+  return LBM_OK;
+}
+
+template <class ST, int G>
+int launch_batch_t(lbm_batch* b, int steps, bool prepare_only) {
+  using Phys = typename BForm<ST>::Phys;
+  const auto kernel = batch_step_kernel<ST, Phys, G>;
+  if (prepare_only) {
+    // Everything that is not a stream operation happens here, outside any graph capture.
+    if (b->table_G != G)
+      if (int rc = build_table<ST>(b, G)) return rc;
+    int grid = b->grid;
+    if (grid <= 0) {
+      int per_sm = 0;
+      B_CUDA(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, b->block, 0));
+      grid = std::max(1, per_sm) * b->sm_count;
+    }
+    b->grid_eff = std::max(1, std::min(grid, (b->items + b->block / 32 - 1) / (b->block / 32)));
+    return LBM_OK;
+  }
+  BatchArgs<ST, Phys> a{};
+  a.mask = b->mask_d;
+  a.inst = static_cast<const BatchInst<typename Phys::Consts>*>(b->table_d);
+  a.count = b->count;
+  a.items = b->items;
+  a.sc = b->sc;
+  for (int s = 0; s < steps; ++s) {
+    a.src = static_cast<const ST*>(b->buf[b->cur]);
+    a.dst = static_cast<ST*>(b->buf[b->cur ^ 1]);
+    kernel<<<b->grid_eff, b->block, 0, b->stream>>>(a);
+    b->cur ^= 1;
+  }
+  const cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+template <class ST>
+int launch_batch(lbm_batch* b, int steps, bool prepare_only) {
+  constexpr int V = StoreTraits<ST>::kVec;
+  constexpr int H = V / 2 >= 2 ? V / 2 : V;  // the narrower vector (8 bytes), FP64 keeps 16
+  const int G = b->G > 0 ? b->G : V;
+  if (G == H && H != V) return launch_batch_t<ST, H>(b, steps, prepare_only);
+  return launch_batch_t<ST, V>(b, steps, prepare_only);
+}
+
+int batch_dispatch(lbm_batch* b, int steps, bool prepare_only) {
+  switch (b->precision) {
+    case LBM_FP32: return launch_batch<float>(b, steps, prepare_only);
+    case LBM_FP64: return launch_batch<double>(b, steps, prepare_only);
+    case LBM_FP16_STORE: return launch_batch<__half>(b, steps, prepare_only);
+    case LBM_BF16_STORE: return launch_batch<__nv_bfloat16>(b, steps, prepare_only);
+    default: return LBM_ERR_INVALID_ARG;
+  }
+}
+
+int batch_steps(lbm_batch* b, int steps) {
+  if (int rc = batch_dispatch(b, 0, true)) return rc;
+  return batch_dispatch(b, steps, false);
+}
+
+// Runs `steps` steps: whole graphs of kGraphSteps launches, then the remainder directly.
+int batch_run(lbm_batch* b, int steps) {
+  if (steps >= kGraphSteps && (b->graph == nullptr || b->graph_cur != b->cur)) {
+    drop_graph(b);
+    if (int rc = batch_dispatch(b, 0, true)) return rc;  // table and grid, outside the capture
+    const int cur0 = b->cur;
+    cudaGraph_t g = nullptr;
+    B_CUDA(b, cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    const int rc = batch_dispatch(b, kGraphSteps, false);
+    const cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (rc || e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();  // the failed capture must not leak into later calls
+      b->cur = cur0;
+      return rc ? rc : bfail(b, LBM_ERR_CUDA, cudaGetErrorString(e));
+    }
+    const cudaError_t ei = cudaGraphInstantiate(&b->graph, g, 0);
+    cudaGraphDestroy(g);
+    if (ei != cudaSuccess) return bfail(b, LBM_ERR_CUDA, cudaGetErrorString(ei));
+    b->cur = cur0;  // capture recorded the launches without running them
+    b->graph_cur = cur0;
+  }
+  while (steps >= kGraphSteps && b->graph) {
+    B_CUDA(b, cudaGraphLaunch(b->graph, b->stream));
+    steps -= kGraphSteps;  // kGraphSteps is even: the current buffer is unchanged
+  }
+  return steps > 0 ? batch_steps(b, steps) : LBM_OK;
+}
+
+template <class ST>
+int separate_t(lbm_batch* b, int steps) {
+  using Phys = typename BForm<ST>::Phys;
+  constexpr int G = StoreTraits<ST>::kVec;
+  std::vector<StepArgs<ST, Phys>> args(b->count);
+  std::vector<int> grids(b->count);
+  const auto kernel = pull_step_kernel<ST, Phys, false, 0>;
+  int per_sm = 0;
+  B_CUDA(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kStepThreads, 0));
+  for (int k = 0; k < b->count; ++k) {
+    const auto& in = b->inst[k];
+    StepArgs<ST, Phys>& a = args[k];
+    a = StepArgs<ST, Phys>{};
+    a.mask = b->mask_d + in.mask_off;
+    a.g = in.g;
+    a.cpr = (in.nx + 32 * G - 1) / (32 * G);
+    a.items = a.cpr * in.ny;
+    a.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
+    a.sc = b->sc;
+    grids[k] = std::max(1, std::min((a.items + kStepThreads / 32 - 1) / (kStepThreads / 32),
+                                    std::max(1, per_sm) * b->sm_count));
+  }
+  for (int s = 0; s < steps; ++s) {
+    const ST* src = static_cast<const ST*>(b->buf[b->cur]);
+    ST* dst = static_cast<ST*>(b->buf[b->cur ^ 1]);
+    for (int k = 0; k < b->count; ++k) {
+      args[k].src = src + b->inst[k].off;
+      args[k].dst = dst + b->inst[k].off;
+      kernel<<<grids[k], kStepThreads, 0, b->stream>>>(args[k]);
+    }
+    b->cur ^= 1;
+  }
+  B_CUDA(b, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int set_inst_t(lbm_batch* b, int k, const void* aos_dev, Eq9<typename StoreTraits<ST>::T> eq) {
+  using T = typename StoreTraits<ST>::T;
+  const auto& in = b->inst[k];
+  const long long n = static_cast<long long>(in.nx) * in.ny;
+  const int grid = static_cast<int>(std::min<long long>((n + 255) / 256, 16LL * b->sm_count));
+  for (int buf = 0; buf < 2; ++buf)
+    set_state_kernel<ST><<<grid, 256, 0, b->stream>>>(static_cast<ST*>(b->buf[buf]) + in.off,
+                                                      b->mask_d + in.mask_off, in.g,
+                                                      static_cast<const T*>(aos_dev), eq, b->sc);
+  B_CUDA(b, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int get_inst_t(lbm_batch* b, int k, void* aos_dev) {
+  using T = typename StoreTraits<ST>::T;
+  const auto& in = b->inst[k];
+  const long long n = static_cast<long long>(in.nx) * in.ny;
+  const int grid = static_cast<int>(std::min<long long>((n + 255) / 256, 16LL * b->sm_count));
+  get_state_kernel<ST><<<grid, 256, 0, b->stream>>>(static_cast<const ST*>(b->buf[b->cur]) + in.off,
+                                                    b->mask_d + in.mask_off, in.g, Eq9<T>{}, b->sc,
+                                                    static_cast<T*>(aos_dev));
+  B_CUDA(b, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
+int mass_inst_t(lbm_batch* b, int k, double* out_dev) {
+  using T = typename StoreTraits<ST>::T;
+  const auto& in = b->inst[k];
+  mass_partial_kernel<ST><<<b->red_blocks, kReduceThreads, 0, b->stream>>>(
+      static_cast<const ST*>(b->buf[b->cur]) + in.off, b->mask_d + in.mask_off, in.g, Eq9<T>{}, b->sc,
+      b->red);
+  mass_final_kernel<<<1, kReduceThreads, 0, b->stream>>>(b->red, b->red_blocks,
+                                                         static_cast<double>(in.fluid), out_dev);
+  B_CUDA(b, cudaGetLastError());
+  return LBM_OK;
+}
+
+int ensure_stage(lbm_batch* b, size_t bytes) {
+  if (b->stage_bytes >= bytes) return LBM_OK;
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  cudaFree(b->stage);
+  b->stage = nullptr;
+  b->stage_bytes = 0;
+  B_CUDA(b, cudaMalloc(&b->stage, bytes));
+  b->stage_bytes = bytes;
+  return LBM_OK;
+}
+
+#define B_DISPATCH(b, fn, ...)                                      \
+  switch ((b)->precision) {                                         \
+    case LBM_FP32: return fn<float>(__VA_ARGS__);                   \
+    case LBM_FP64: return fn<double>(__VA_ARGS__);                  \
+    case LBM_FP16_STORE: return fn<__half>(__VA_ARGS__);            \
+    case LBM_BF16_STORE: return fn<__nv_bfloat16>(__VA_ARGS__);     \
+    default: return bfail(b, LBM_ERR_INVALID_ARG, "bad precision"); \
+  }
+
+template <class ST>
+int init_eq_t(lbm_batch* b, double rho0, double ux0, double uy0) {
+  using T = typename StoreTraits<ST>::T;
+  Eq9<T> e{};
+  const T r = T(rho0), u = T(ux0), v = T(uy0);
+  const T usq = u * u + v * v, drho0 = r - T(1);
+  static const int cx[kQ] = {0, 1, 0, -1, 0, 1, -1, -1, 1}, cy[kQ] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
+  for (int i = 0; i < kQ; ++i) {
+    const T cu = cx[i] * u + cy[i] * v;
+    e.v[i] = weight<T>(i) * (drho0 + r * (T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq));
+  }
+  for (int k = 0; k < b->count; ++k)
+    if (int rc = set_inst_t<ST>(b, k, nullptr, e)) return rc;
+  return LBM_OK;
+}
+
+template <class ST>
+int set_pop_t(lbm_batch* b, int k, const void* host) {
+  using T = typename StoreTraits<ST>::T;
+  const auto& in = b->inst[k];
+  const size_t bytes = static_cast<size_t>(in.nx) * in.ny * kQ * sizeof(T);
+  if (int rc = ensure_stage(b, bytes)) return rc;
+  B_CUDA(b, cudaMemcpyAsync(b->stage, host, bytes, cudaMemcpyHostToDevice, b->stream));
+  if (int rc = set_inst_t<ST>(b, k, b->stage, Eq9<T>{})) return rc;
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
+template <class ST>
+int get_pop_t(lbm_batch* b, int k, void* host) {
+  using T = typename StoreTraits<ST>::T;
+  const auto& in = b->inst[k];
+  const size_t bytes = static_cast<size_t>(in.nx) * in.ny * kQ * sizeof(T);
+  if (int rc = ensure_stage(b, bytes)) return rc;
+  if (int rc = get_inst_t<ST>(b, k, b->stage)) return rc;
+  B_CUDA(b, cudaMemcpyAsync(host, b->stage, bytes, cudaMemcpyDeviceToHost, b->stream));
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
+int time_steps(lbm_batch* b, int steps, double* seconds) {
+  B_CUDA(b, cudaEventRecord(b->ev[0], b->stream));
+  if (int rc = batch_run(b, steps)) return rc;
+  B_CUDA(b, cudaEventRecord(b->ev[1], b->stream));
+  B_CUDA(b, cudaEventSynchronize(b->ev[1]));
+  float ms = 0.f;
+  B_CUDA(b, cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+  *seconds = ms * 1e-3;
+  return LBM_OK;
+}
+
+std::string tune_key(const lbm_batch* b) {
+  cudaDeviceProp prop{};
+  cudaGetDeviceProperties(&prop, b->device);
+  std::ostringstream k;
+  k << prop.name << "|p" << b->precision << "|n" << b->count << "|c" << b->total_cells;
+  return k.str();
+}
+
+}  // namespace
+
+extern "C" {
+
+int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* const* solid,
+                     const double* tau, const double* fx, const double* fy, int precision,
+                     lbm_batch** out) {
+  if (!out) return LBM_ERR_INVALID_ARG;
+  *out = nullptr;
+  const int elem = element_bytes(precision);
+  if (count < 1 || count > kBatchMaxInstances || !nx || !ny || !solid || !tau || !fx || !fy || !elem)
+    return LBM_ERR_INVALID_ARG;
+  for (int k = 0; k < count; ++k) {
+    const bool tau_ok = precision == LBM_FP64 ? tau[k] > 0.5 : static_cast<float>(tau[k]) > 0.5f;
+    if (nx[k] < 1 || ny[k] < 1 || !solid[k] || !tau_ok) return LBM_ERR_INVALID_ARG;
+  }
+  lbm_batch* b = new (std::nothrow) lbm_batch();
+  if (!b) return LBM_ERR_OUT_OF_MEMORY;
+  b->precision = precision;
+  b->elem = elem;
+  b->vec = 16 / elem;
+  b->host_elem = precision == LBM_FP64 ? 8 : 4;
+  b->count = count;
+  b->inst.resize(count);
+  for (int i = 0; i < kQ; ++i) {
+    const int e = (precision == LBM_FP16_STORE || precision == LBM_BF16_STORE) ? (i == 0 ? 15 : (i <= 4 ? 17 : 18)) : 0;
+    b->sc.enc[i] = std::ldexp(1.0f, e);
+    b->sc.dec[i] = std::ldexp(1.0f, -e);
+  }
+  auto fail = [&](int code) {
+    lbm_batch_destroy(b);
+    return code;
+  };
+  long long off = 0, moff = 0;
+  std::vector<uint32_t> words;
+  std::vector<uint32_t> all_words;
+  const int per_line = 128 / elem;
+  for (int k = 0; k < count; ++k) {
+    auto& in = b->inst[k];
+    in.nx = nx[k];
+    in.ny = ny[k];
+    in.tau = tau[k];
+    in.fx = fx[k];
+    in.fy = fy[k];
+    in.g.nx = nx[k];
+    in.g.ny = ny[k];
+    in.g.pitch = (nx[k] + per_line - 1) / per_line * per_line;
+    const int span = 32 * b->vec;
+    in.g.mask_words = (nx[k] + span - 1) / span * b->vec + 2;
+    in.g.plane = static_cast<long long>(in.g.pitch) * ny[k];
+    in.g.open_x = 0;
+    in.off = off;
+    in.mask_off = moff;
+    in.fluid = 0;
+    const size_t n = static_cast<size_t>(nx[k]) * ny[k];
+    for (size_t c = 0; c < n; ++c) in.fluid += solid[k][c] ? 0 : 1;
+    pack_mask(solid[k], nx[k], ny[k], in.g.mask_words, words);
+    all_words.insert(all_words.end(), words.begin(), words.end());
+    off += kQ * in.g.plane;
+    moff += static_cast<long long>(in.g.mask_words) * ny[k];
+    b->total_cells += static_cast<long long>(nx[k]) * ny[k];
+  }
+  b->total_elems = off;
+  if (cudaGetDevice(&b->device) != cudaSuccess ||
+      cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&b->ev[0]) != cudaSuccess || cudaEventCreate(&b->ev[1]) != cudaSuccess)
+    return fail(LBM_ERR_CUDA);
+  const size_t bytes = static_cast<size_t>(off) * elem + 256;
+  cudaError_t e = cudaSuccess;
+  for (int k = 0; k < 2 && e == cudaSuccess; ++k) {
+    e = cudaMalloc(&b->buf[k], bytes);
+    if (e == cudaSuccess) e = cudaMemset(b->buf[k], 0, bytes);
+  }
+  if (e == cudaSuccess) e = cudaMalloc(&b->mask_d, all_words.size() * sizeof(uint32_t));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(b->mask_d, all_words.data(), all_words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
+  b->red_blocks = 4 * b->sm_count;
+  if (e == cudaSuccess) e = cudaMalloc(&b->red, (b->red_blocks + 2) * sizeof(double));
+  if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
+  *out = b;
+  return LBM_OK;
+}
+
+int lbm_batch_destroy(lbm_batch* b) {
+  if (!b) return LBM_OK;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  drop_graph(b);
+  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->stage,
+                  static_cast<void*>(b->red)})
+    cudaFree(p);
+  for (cudaEvent_t ev : b->ev)
+    if (ev) cudaEventDestroy(ev);
+  if (b->stream) cudaStreamDestroy(b->stream);
+  delete b;
+  return LBM_OK;
+}
+
+const char* lbm_batch_last_error(const lbm_batch* b) { return b ? b->err.c_str() : "null"; }
+
+int lbm_batch_init_equilibrium(lbm_batch* b, double rho0, double ux0, double uy0) {
+  if (!b) return LBM_ERR_INVALID_ARG;
+  B_DISPATCH(b, init_eq_t, b, rho0, ux0, uy0);
+}
+
+int lbm_batch_set_populations(lbm_batch* b, int instance, const void* s_host) {
+  if (!b || !s_host || instance < 0 || instance >= b->count)
+    return bfail(b, LBM_ERR_INVALID_ARG, "bad instance or null state");
+  B_DISPATCH(b, set_pop_t, b, instance, s_host);
+}
+
+int lbm_batch_get_populations(lbm_batch* b, int instance, void* s_host) {
+  if (!b || !s_host || instance < 0 || instance >= b->count)
+    return bfail(b, LBM_ERR_INVALID_ARG, "bad instance or null output");
+  B_DISPATCH(b, get_pop_t, b, instance, s_host);
+}
+
+int lbm_batch_total_mass(lbm_batch* b, int instance, double* mass) {
+  if (!b || !mass || instance < 0 || instance >= b->count)
+    return bfail(b, LBM_ERR_INVALID_ARG, "bad instance or null output");
+  int rc;
+  double* out = b->red + b->red_blocks;
+  switch (b->precision) {
+    case LBM_FP32: rc = mass_inst_t<float>(b, instance, out); break;
+    case LBM_FP64: rc = mass_inst_t<double>(b, instance, out); break;
+    case LBM_FP16_STORE: rc = mass_inst_t<__half>(b, instance, out); break;
+    default: rc = mass_inst_t<__nv_bfloat16>(b, instance, out); break;
+  }
+  if (rc) return rc;
+  B_CUDA(b, cudaMemcpyAsync(mass, out, sizeof(double), cudaMemcpyDeviceToHost, b->stream));
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
+int lbm_batch_run(lbm_batch* b, int steps) {
+  if (!b || steps < 0) return bfail(b, LBM_ERR_INVALID_ARG, "steps must be >= 0");
+  if (int rc = batch_run(b, steps)) return rc;
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  return LBM_OK;
+}
+
+int lbm_batch_timed_run(lbm_batch* b, int steps, double* seconds) {
+  if (!b || !seconds || steps < 0) return bfail(b, LBM_ERR_INVALID_ARG, "bad arguments");
+  return time_steps(b, steps, seconds);
+}
+
+int lbm_batch_run_separate(lbm_batch* b, int steps, double* seconds) {
+  if (!b || steps < 0) return bfail(b, LBM_ERR_INVALID_ARG, "steps must be >= 0");
+  B_CUDA(b, cudaEventRecord(b->ev[0], b->stream));
+  int rc;
+  switch (b->precision) {
+    case LBM_FP32: rc = separate_t<float>(b, steps); break;
+    case LBM_FP64: rc = separate_t<double>(b, steps); break;
+    case LBM_FP16_STORE: rc = separate_t<__half>(b, steps); break;
+    default: rc = separate_t<__nv_bfloat16>(b, steps); break;
+  }
+  if (rc) return rc;
+  B_CUDA(b, cudaEventRecord(b->ev[1], b->stream));
+  B_CUDA(b, cudaEventSynchronize(b->ev[1]));
+  float ms = 0.f;
+  B_CUDA(b, cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
+  if (seconds) *seconds = ms * 1e-3;
+  drop_graph(b);  // the current buffer may have changed parity
+  return LBM_OK;
+}
+
+int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, int grid_blocks) {
+  if (!b) return LBM_ERR_INVALID_ARG;
+  const int V = b->vec, H = V / 2 >= 2 ? V / 2 : V;
+  if ((cells_per_thread != 0 && cells_per_thread != V && cells_per_thread != H) ||
+      block_threads % 32 != 0 || block_threads <= 0 || block_threads > kBatchThreads || grid_blocks < 0)
+    return bfail(b, LBM_ERR_INVALID_ARG, "bad launch configuration");
+  b->G = cells_per_thread;
+  b->block = block_threads;
+  b->grid = grid_blocks;
+  drop_graph(b);
+  return LBM_OK;
+}
+
+int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_t report_size) {
+  if (!b) return LBM_ERR_INVALID_ARG;
+  const std::string key = tune_key(b);
+  // Cached choice?
+  if (cache_path) {
+    std::ifstream in(cache_path);
+    std::string line;
+    while (std::getline(in, line)) {
+      std::istringstream ls(line);
+      std::string k;
+      int G, blk, grd;
+      if (std::getline(ls, k, '\t') && k == key && (ls >> G >> blk >> grd)) {
+        if (lbm_batch_set_launch(b, G, blk, grd) == LBM_OK) {
+          b->tune_report = "cached: G=" + std::to_string(G) + " block=" + std::to_string(blk) +
+                           " grid=" + std::to_string(grd);
+          if (report && report_size) std::snprintf(report, report_size, "%s", b->tune_report.c_str());
+          return LBM_OK;
+        }
+      }
+    }
+  }
+  // Time every candidate on the current state; the state advances, which is harmless for
+  // timing and is restored below by re-running the same number of steps from a saved copy.
+  const size_t bytes = static_cast<size_t>(b->total_elems) * b->elem + 256;
+  void* saved = nullptr;
+  B_CUDA(b, cudaMalloc(&saved, bytes));
+  B_CUDA(b, cudaMemcpyAsync(saved, b->buf[b->cur], bytes, cudaMemcpyDeviceToDevice, b->stream));
+  const int V = b->vec, H = V / 2 >= 2 ? V / 2 : V;
+  struct Cand {
+    int G, blk, per_sm;
+    double t;
+  };
+  std::vector<Cand> cands;
+  for (int G : {V, H}) {
+    if (G == H && H == V && !cands.empty() && cands.back().G == G) continue;
+    for (int blk : {128, 256})
+      for (int per_sm : {1, 2, 4, 8}) cands.push_back({G, blk, per_sm, 0.0});
+  }
+  double best = 1e30;
+  Cand pick = cands.front();
+  std::ostringstream rep;
+  for (Cand& c : cands) {
+    if (int rc = lbm_batch_set_launch(b, c.G, c.blk, c.per_sm * b->sm_count)) {
+      cudaFree(saved);
+      return rc;
+    }
+    double t = 0.0;
+    if (int rc = time_steps(b, 4, &t)) {  // warm-up
+      cudaFree(saved);
+      return rc;
+    }
+    if (int rc = time_steps(b, 16, &t)) {
+      cudaFree(saved);
+      return rc;
+    }
+    c.t = t;
+    rep << "G" << c.G << "/b" << c.blk << "/x" << c.per_sm << ":" << static_cast<long long>(b->total_cells * 16 / t / 1e6)
+        << " ";
+    if (t < best) {
+      best = t;
+      pick = c;
+    }
+  }
+  B_CUDA(b, cudaMemcpyAsync(b->buf[b->cur], saved, bytes, cudaMemcpyDeviceToDevice, b->stream));
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  cudaFree(saved);
+  if (int rc = lbm_batch_set_launch(b, pick.G, pick.blk, pick.per_sm * b->sm_count)) return rc;
+  b->tune_report = "tuned: G=" + std::to_string(pick.G) + " block=" + std::to_string(pick.blk) +
+                   " grid=" + std::to_string(pick.per_sm * b->sm_count) + " | " + rep.str();
+  if (cache_path) {
+    std::ofstream outf(cache_path, std::ios::app);
+    outf << key << '\t' << pick.G << ' ' << pick.blk << ' ' << pick.per_sm * b->sm_count << '\n';
+  }
+  if (report && report_size) std::snprintf(report, report_size, "%s", b->tune_report.c_str());
+  return LBM_OK;
+}
+
+int lbm_batch_info(const lbm_batch* b, int* count, long long* total_cells, int* items) {
+  if (!b) return LBM_ERR_INVALID_ARG;
+  if (count) *count = b->count;
+  if (total_cells) *total_cells = b->total_cells;
+  if (items) *items = b->items;
+  return LBM_OK;
+}
+
+}  // extern "C"

@@ -31,6 +31,9 @@ namespace lbm_b200 {
 // bit. Host fallbacks keep the templates instantiable on the host side of the translation unit.
 struct ExactF32 {
   using T = float;
+  using S = float;
+  static __host__ __device__ __forceinline__ float k(float v) { return v; }
+  static __host__ __device__ __forceinline__ float neg(float a) { return -a; }
   static __host__ __device__ __forceinline__ float add(float a, float b) {
 #ifdef __CUDA_ARCH__
     return __fadd_rn(a, b);
@@ -63,6 +66,9 @@ struct ExactF32 {
 
 struct ExactF64 {
   using T = double;
+  using S = double;
+  static __host__ __device__ __forceinline__ double k(double v) { return v; }
+  static __host__ __device__ __forceinline__ double neg(double a) { return -a; }
   static __host__ __device__ __forceinline__ double add(double a, double b) {
 #ifdef __CUDA_ARCH__
     return __dadd_rn(a, b);
@@ -91,6 +97,18 @@ struct ExactF64 {
     return a / b;
 #endif
   }
+};
+
+// Packed arithmetic of the fast collision (two cells per instruction).
+struct FastF32x2 {
+  using T = float2;
+  static __device__ __forceinline__ float2 k(float v) { return make_float2(v, v); }
+  static __device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+  static __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+  static __device__ __forceinline__ float2 sub(float2 a, float2 b) { return __fadd2_rn(a, neg(b)); }
+  static __device__ __forceinline__ float2 mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+  static __device__ __forceinline__ float2 fma(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
+  static __device__ __forceinline__ float2 rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 };
 
 // ---------------------------------------------------------------------------------------------
@@ -246,6 +264,67 @@ __device__ __forceinline__ void store_vec<__nv_bfloat16>(__nv_bfloat16* p, const
                                                          int i, const PlaneScales& s) {
   store_vec16(p, v, i, s);
 }
+
+// G consecutive cells as one aligned vector of G * sizeof(ST) bytes (8 or 16), decoded /
+// encoded; generalises load_vec / store_vec to the narrower vectors of the cells-per-thread
+// tuning dimension.
+template <class ST, int G>
+struct VecIO;
+template <class ST>
+struct VecIO<ST, StoreTraits<ST>::kVec> {
+  using T = typename StoreTraits<ST>::T;
+  static constexpr int G = StoreTraits<ST>::kVec;
+  static __device__ __forceinline__ void load(const ST* p, T (&v)[G], int i, const PlaneScales& s) {
+    load_vec<ST>(p, v, i, s);
+  }
+  static __device__ __forceinline__ void store(ST* p, const T (&v)[G], int i, const PlaneScales& s) {
+    store_vec<ST>(p, v, i, s);
+  }
+};
+template <>
+struct VecIO<float, 2> {
+  static __device__ __forceinline__ void load(const float* p, float (&v)[2], int, const PlaneScales&) {
+    const float2 t = __ldg(reinterpret_cast<const float2*>(p));
+    v[0] = t.x;
+    v[1] = t.y;
+  }
+  static __device__ __forceinline__ void store(float* p, const float (&v)[2], int, const PlaneScales&) {
+    *reinterpret_cast<float2*>(p) = make_float2(v[0], v[1]);
+  }
+};
+template <class H>
+struct VecIO16x4 {
+  static __device__ __forceinline__ void load(const H* p, float (&v)[4], int i, const PlaneScales& s) {
+    const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
+    const uint32_t w[2] = {t.x, t.y};
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      H lo, hi;
+      const uint16_t a = static_cast<uint16_t>(w[k] & 0xffffu), b = static_cast<uint16_t>(w[k] >> 16);
+      memcpy(&lo, &a, 2);
+      memcpy(&hi, &b, 2);
+      v[2 * k] = to_float(lo) * s.dec[i];
+      v[2 * k + 1] = to_float(hi) * s.dec[i];
+    }
+  }
+  static __device__ __forceinline__ void store(H* p, const float (&v)[4], int i, const PlaneScales& s) {
+    uint32_t w[2];
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      const H lo = from_float<H>(v[2 * k] * s.enc[i]);
+      const H hi = from_float<H>(v[2 * k + 1] * s.enc[i]);
+      uint16_t a, b;
+      memcpy(&a, &lo, 2);
+      memcpy(&b, &hi, 2);
+      w[k] = static_cast<uint32_t>(a) | (static_cast<uint32_t>(b) << 16);
+    }
+    *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+  }
+};
+template <>
+struct VecIO<__half, 4> : VecIO16x4<__half> {};
+template <>
+struct VecIO<__nv_bfloat16, 4> : VecIO16x4<__nv_bfloat16> {};
 
 template <class ST>
 __device__ __forceinline__ typename StoreTraits<ST>::T load_one(const ST* p, int i,

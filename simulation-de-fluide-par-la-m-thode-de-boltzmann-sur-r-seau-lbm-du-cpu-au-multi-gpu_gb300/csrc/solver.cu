@@ -18,6 +18,7 @@
 #include "lbm_b200.h"
 #include "solver_internal.h"
 #include "step_kernel.cuh"
+#include "step_tma.cuh"
 
 using namespace lbm_b200;
 
@@ -29,25 +30,33 @@ template <>
 struct Form<float> {
   using A = ExactF32;
   using Phys = ExactPhys<ExactF32>;
-  static constexpr const char* name = "fp32";
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_collide_consts<float>(float(tau), float(fx), float(fy));
+  }
 };
 template <>
 struct Form<double> {
   using A = ExactF64;
   using Phys = ExactPhys<ExactF64>;
-  static constexpr const char* name = "fp64";
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_collide_consts<double>(tau, fx, fy);
+  }
 };
 template <>
 struct Form<__half> {
-  using A = ExactF32;
-  using Phys = ExactPhys<ExactF32>;
-  static constexpr const char* name = "fp16_store";
+  using A = ExactF32;  // moment pass
+  using Phys = FastPhys;
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_fast_consts(float(tau), float(fx), float(fy));
+  }
 };
 template <>
 struct Form<__nv_bfloat16> {
   using A = ExactF32;
-  using Phys = ExactPhys<ExactF32>;
-  static constexpr const char* name = "bf16_store";
+  using Phys = FastPhys;
+  static Phys::Consts consts(double tau, double fx, double fy) {
+    return make_fast_consts(float(tau), float(fx), float(fy));
+  }
 };
 
 constexpr int kCx[kQ] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
@@ -96,7 +105,7 @@ Eq9<typename StoreTraits<ST>::T> inlet_eq(const lbm_solver* s) {
   return host_equilibrium<T>(T(1), T(s->u_in), T(0));
 }
 
-template <class ST, bool kOpen>
+template <class ST, bool kOpen, int kVariant>
 int launch_steps_t(lbm_solver* s, int steps) {
   using Phys = typename Form<ST>::Phys;
   using T = typename StoreTraits<ST>::T;
@@ -106,11 +115,11 @@ int launch_steps_t(lbm_solver* s, int steps) {
   a.g = s->g;
   a.cpr = (s->nx + 32 * G - 1) / (32 * G);
   a.items = s->ny * a.cpr;
-  a.k = make_collide_consts<T>(T(s->tau), T(s->fx), T(s->fy));
+  a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
   const Eq9<T> e = inlet_eq<ST>(s);
   for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
   a.sc = s->sc;
-  const auto kernel = pull_step_kernel<ST, Phys, kOpen>;
+  const auto kernel = pull_step_kernel<ST, Phys, kOpen, kVariant>;
   int grid = s->grid;
   if (grid <= 0) {
     int per_sm = 0;
@@ -130,9 +139,71 @@ int launch_steps_t(lbm_solver* s, int steps) {
   return LBM_OK;
 }
 
+// Warp-specialised bulk-copy step (step_tma.cuh) with kStages ring stages.
+template <class ST, bool kOpen, int kStages>
+int launch_tma_t(lbm_solver* s, int steps) {
+  using Phys = typename Form<ST>::Phys;
+  using T = typename StoreTraits<ST>::T;
+  using S = TmaShape<ST>;
+  StepArgs<ST, Phys> a{};
+  a.mask = s->mask_d;
+  a.g = s->g;
+  a.cpr = (s->nx + 32 * S::G - 1) / (32 * S::G);
+  a.items = s->ny * a.cpr;
+  a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
+  const Eq9<T> e = inlet_eq<ST>(s);
+  for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
+  a.sc = s->sc;
+  const int tpr = (s->nx + S::TW - 1) / S::TW;
+  const int tiles = tpr * s->ny;
+  const auto kernel = pull_step_tma_kernel<ST, Phys, kOpen, kStages>;
+  const size_t smem = tma_smem_bytes<ST>(kStages);
+  LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+  int grid = s->grid;
+  if (grid <= 0) {
+    int per_sm = 0;
+    LBM_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kTmaThreads, smem));
+    grid = std::max(1, std::min(tiles, std::max(1, per_sm) * s->sm_count));
+  }
+  s->last_grid = grid;
+  for (int k = 0; k < steps; ++k) {
+    a.src = static_cast<const ST*>(s->buf[s->cur]);
+    a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+    kernel<<<grid, kTmaThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
+    s->cur ^= 1;
+  }
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+// Automatic kernel choice (variant < 0): the warp-specialised ring (4) when the rows hold whole
+// 1024-cell-class tiles and there are enough tiles to fill the GPU, the direct kernel (0)
+// otherwise (narrow or small grids, where most consumer warps of a tile would idle).
+template <class ST>
+int auto_variant(const lbm_solver* s) {
+  using S = TmaShape<ST>;
+  const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
+  return (s->nx >= S::TW && tiles >= 4LL * s->sm_count) ? 4 : 0;
+}
+
+template <class ST, bool kOpen>
+int launch_steps_o(lbm_solver* s, int steps) {
+  s->last_variant = s->variant >= 0 ? s->variant : auto_variant<ST>(s);
+  switch (s->last_variant) {
+    case 1: return launch_steps_t<ST, kOpen, 1>(s, steps);
+    case 2: return launch_steps_t<ST, kOpen, 2>(s, steps);
+    case 3: return launch_steps_t<ST, kOpen, 3>(s, steps);
+    case 4: return launch_tma_t<ST, kOpen, 2>(s, steps);
+    case 5: return launch_tma_t<ST, kOpen, 3>(s, steps);
+    case 6: return launch_tma_t<ST, kOpen, 4>(s, steps);
+    default: return launch_steps_t<ST, kOpen, 0>(s, steps);
+  }
+}
+
 template <class ST>
 int launch_steps(lbm_solver* s, int steps) {
-  return s->open_x ? launch_steps_t<ST, true>(s, steps) : launch_steps_t<ST, false>(s, steps);
+  return s->open_x ? launch_steps_o<ST, true>(s, steps) : launch_steps_o<ST, false>(s, steps);
 }
 
 template <class ST>
@@ -328,11 +399,16 @@ int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, doub
 
   const int per_line = 128 / elem;
   const int pitch = (nx + per_line - 1) / per_line * per_line;
-  const int cpr = (nx + 32 * s->vec - 1) / (32 * s->vec);
+  // Mask rows cover whole tiles of the widest kernel (a warp-specialised tile is kConsumers
+  // chunks of 32 * vec cells) plus the 4 words its bulk copy of a tile's mask row reads past the
+  // tile; lanes past the row end read their (all-solid) window. The word count is a multiple of
+  // 4 so that every row starts on a 16-byte boundary (bulk-copy alignment).
+  const int span = kConsumers * 32 * s->vec;
+  const int tiles_per_row = (nx + span - 1) / span;
   s->g.nx = nx;
   s->g.ny = ny;
   s->g.pitch = pitch;
-  s->g.mask_words = cpr * s->vec + 2;
+  s->g.mask_words = tiles_per_row * span / 32 + 4;
   s->g.plane = static_cast<long long>(pitch) * ny;
   s->g.open_x = 0;
 
@@ -367,6 +443,8 @@ int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, doub
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
   s->red_blocks = 4 * s->sm_count;
   e = cudaMalloc(&s->red, (s->red_blocks + 2) * sizeof(double) + 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->red, 0, (s->red_blocks + 2) * sizeof(double) + 2 * sizeof(int), s->stream);
+  s->err_flag = reinterpret_cast<int*>(s->red + s->red_blocks + 2) + 1;
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
   e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
@@ -439,10 +517,23 @@ int lbm_step(lbm_solver* s, int steps) {
   return lbm_b200::solver_step_raw(s, steps);
 }
 
+// Reads and clears the device error flag of the step kernels (a bounded wait that ran out).
+int check_step_flag(lbm_solver* s) {
+  int flag = 0;
+  LBM_CUDA(s, cudaMemcpyAsync(&flag, s->err_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  if (flag) {
+    LBM_CUDA(s, cudaMemsetAsync(s->err_flag, 0, sizeof(int), s->stream));
+    LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+    return set_error(s, LBM_ERR_TIMEOUT, "a step kernel gave up waiting for its shared-memory ring");
+  }
+  return LBM_OK;
+}
+
 int lbm_synchronize(lbm_solver* s) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
   LBM_CUDA(s, cudaStreamSynchronize(s->stream));
-  return LBM_OK;
+  return check_step_flag(s);
 }
 
 int lbm_run(lbm_solver* s, int steps) {
@@ -459,7 +550,7 @@ int lbm_timed_run(lbm_solver* s, int steps, double* seconds) {
   float ms = 0.f;
   LBM_CUDA(s, cudaEventElapsedTime(&ms, s->ev[0], s->ev[1]));
   *seconds = static_cast<double>(ms) * 1e-3;
-  return LBM_OK;
+  return check_step_flag(s);
 }
 
 int lbm_get_populations(lbm_solver* s, void* s_host) {
@@ -565,7 +656,8 @@ int lbm_device_info(lbm_solver* s, char* buf, size_t size) {
       ver(CUDART_VERSION) + "\", \"ecc\": " + std::to_string(prop.ECCEnabled) +
       ", \"sm_count\": " + std::to_string(s->sm_count) + ", \"block\": \"" +
       std::to_string(s->block) + "x1\", \"grid\": " + std::to_string(s->last_grid) +
-      ", \"variant\": \"b200_pull_vec" + std::to_string(s->vec) + "\", \"precision\": \"" +
+      ", \"variant\": \"b200_pull_vec" + std::to_string(s->vec) +
+      "_v" + std::to_string(s->last_variant) + (s->variant < 0 ? "_auto" : "") + "\", \"precision\": \"" +
       names[s->precision] + "\"";
   std::snprintf(buf, size, "%s", info.c_str());
   return LBM_OK;
@@ -586,6 +678,14 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
     return set_error(s, LBM_ERR_INVALID_ARG, "block must be a multiple of 32 and <= 256");
   s->block = block_threads;
   s->grid = grid_blocks;
+  return LBM_OK;
+}
+
+int lbm_set_variant(lbm_solver* s, int variant) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  if (variant < -1 || variant >= kStepVariants + 3)
+    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 7)");
+  s->variant = variant;
   return LBM_OK;
 }
 

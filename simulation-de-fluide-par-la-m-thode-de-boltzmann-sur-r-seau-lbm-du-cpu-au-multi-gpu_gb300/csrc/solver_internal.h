@@ -31,6 +31,9 @@ struct lbm_solver {
   void* stage = nullptr;  // device staging for host input / output
   size_t stage_bytes = 0;
   int block = 256, grid = 0, last_grid = 0;  // step launch shape (grid 0: persistent, automatic)
+  int* err_flag = nullptr;  // set by a step kernel whose bounded wait ran out
+  int variant = -1;      // step kernel variant (lbm_set_variant); -1: chosen from the grid shape
+  int last_variant = 0;  // variant of the last launch
   int device = 0, sm_count = 0;
   lbm_b200::PlaneScales sc{};
   std::string err;

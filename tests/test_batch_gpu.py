@@ -1,0 +1,79 @@
+"""Batched ensemble (GPU): uneven closed channels stepped by one persistent launch per step.
+
+Workload shape: seeded channels nx ~ U[64, 1024], ny ~ U[32, 512], 1-4 discs of radius 4-24
+clear of the walls, tau ~ U[0.52, 1.0], fx ~ U[1e-6, 1e-5], seeded initial perturbation.
+Checks: 8 sampled instances bit-exact against the oracle's port of the reference v1 solver (itself
+pinned bit for bit to the reference v0); batched == one launch per instance, every launch shape;
+the autotuner leaves the state unchanged; the FP16-storage batch stays close to FP32.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+COUNT, STEPS = 24, 300
+
+
+@pytest.fixture(scope="module")
+def specs(gpu_lib):
+    return gpu_lib.workloads.ensemble_specs(COUNT, seed=11)
+
+
+def _fill(b, specs, orc, real="f32"):
+    for k, s in enumerate(specs):
+        b.set_populations(k, orc.seeded_state(s["seed"], 1e-4, s["nx"], s["ny"], s["mask"], real))
+
+
+def test_sampled_instances_bit_exact(gpu_lib, orc, specs):
+    with gpu_lib.Batch(specs, precision="fp32") as b:
+        _fill(b, specs, orc)
+        b.run(STEPS)
+        picks = np.linspace(0, COUNT - 1, 8).astype(int)
+        for k in picks:
+            s = specs[k]
+            nx, ny, m = s["nx"], s["ny"], s["mask"]
+            r = orc.s_to_r(nx, ny, m, orc.seeded_state(s["seed"], 1e-4, nx, ny, m))
+            orc.pull_run(nx, ny, m, float(np.float32(s["tau"])), s["fx"], 0.0, r, STEPS)
+            want = orc.r_to_s(nx, ny, m, r)
+            assert np.array_equal(b.populations(k), want), f"instance {k} ({nx}x{ny})"
+
+
+@pytest.mark.parametrize("launch", [(0, 256, 0), (2, 128, 0), (4, 64, 300), (2, 256, 152)])
+def test_batched_equals_separate_launches(gpu_lib, orc, specs, launch):
+    with gpu_lib.Batch(specs) as a, gpu_lib.Batch(specs) as b:
+        _fill(a, specs, orc)
+        _fill(b, specs, orc)
+        a.set_launch(*launch)
+        a.run(130)  # graph replays (64 steps each) and a direct remainder
+        b.run_separate(130)
+        for k in range(COUNT):
+            assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k}"
+
+
+def test_autotune_keeps_state(gpu_lib, orc, specs, tmp_path):
+    cache = tmp_path / "tune.txt"
+    with gpu_lib.Batch(specs) as b:
+        _fill(b, specs, orc)
+        b.run(10)
+        before = [b.populations(k) for k in (0, COUNT - 1)]
+        report = b.autotune(cache)
+        assert report.startswith("tuned")
+        after = [b.populations(k) for k in (0, COUNT - 1)]
+        assert all(np.array_equal(x, y) for x, y in zip(before, after))
+        assert b.autotune(cache).startswith("cached")
+
+
+def test_fp16_batch_close_to_fp32(gpu_lib, orc, specs):
+    sub = specs[:6]
+    with gpu_lib.Batch(sub, precision="fp32") as a, gpu_lib.Batch(sub, precision="fp16") as h:
+        _fill(a, sub, orc)
+        _fill(h, sub, orc)
+        a.run(200)
+        h.run(200)
+        for k in range(len(sub)):
+            x, y = a.populations(k), h.populations(k)
+            assert np.linalg.norm(x - y) / np.linalg.norm(x) < 5e-3
+        for k in range(len(sub)):
+            assert abs(h.total_mass(k) - a.total_mass(k)) / a.total_mass(k) < 1e-5
