@@ -143,8 +143,17 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * current one is computed (more bytes in flight, more registers); 2 and 3 cap the registers for
  * 4 and 3 resident blocks per SM. 4, 5, 6: warp-specialised kernel, a producer warp streams
  * tiles into a shared-memory ring of 2, 3, 4 stages with bulk asynchronous copies (TMA) and
- * eight consumer warps collide from shared memory. -1 (the default): 4 for grids whose rows hold
- * whole tiles and enough tiles to fill the GPU, 0 otherwise. */
+ * eight consumer warps collide from shared memory. 7 and 8: variants 4 and 0 with the FP32
+ * collision computed for two cells per packed instruction (other precisions: same as 4 and 0).
+ * 9, 10, 11: per-warp pipeline, each warp keeps 2, 3, 4 chunks in flight in its own
+ * shared-memory ring with 16-byte asynchronous copies (packed FP32 collision). 12..16: producer
+ * warp and bulk-copy ring as in 4, consumers with one cell per lane and consecutive lanes on
+ * consecutive cells (plain FP32 / FP64 storage; the 16-bit forms run 4): 12 = 8 consumer warps x
+ * 64-cell strips, 2 stages; 13 = the same with 3 stages; 14 = 12 capped at 56 registers for 4
+ * resident blocks; 15 = 4 consumer warps, 3 stages; 16 = 15 capped for 7 resident blocks.
+ * -1 (the default): plain FP32 / FP64 run 12 when there are at least two of its 512-cell
+ * (FP64: 512-cell) tiles per SM, 0 otherwise; the 16-bit forms run 4 when the rows hold whole
+ * tiles and there are enough tiles to fill the GPU, 0 otherwise. */
 int lbm_set_variant(lbm_solver* s, int variant);
 
 /* Device memory of the two population buffers (for zero-copy consumers): plane stride and row

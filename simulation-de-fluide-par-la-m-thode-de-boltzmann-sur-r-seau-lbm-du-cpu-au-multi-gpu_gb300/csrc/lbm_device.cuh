@@ -99,6 +99,29 @@ struct ExactF64 {
   }
 };
 
+// Exact FP32 arithmetic on two cells per instruction (packed add.rn.f32x2 / fma.rn.f32x2).
+// Each packed operation is correctly rounded per lane, like the scalar one, but the compiler
+// contracts a packed multiply feeding a packed add into one fused multiply-add even when both
+// carry an explicit rounding mode (measured: 3a + 4.5aa differs from the two-rounding result in
+// 25% of random pairs, the rate of contraction). So the multiply is written as a fused
+// multiply-add with a -0 addend, round(a*b + -0) = round(a*b) for every a, b (a zero product
+// keeps its sign), and the -0 comes from constant memory, a value the compiler cannot see
+// through: nothing is left to contract. Division stays per lane (__fdiv_rn).
+static __constant__ float2 kNegZero2 = {-0.0f, -0.0f};
+
+struct ExactF32x2 {
+  using T = float2;
+  using S = float;
+  static __device__ __forceinline__ float2 k(float v) { return make_float2(v, v); }
+  static __device__ __forceinline__ float2 neg(float2 a) { return make_float2(-a.x, -a.y); }
+  static __device__ __forceinline__ float2 add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+  static __device__ __forceinline__ float2 sub(float2 a, float2 b) { return __fadd2_rn(a, neg(b)); }
+  static __device__ __forceinline__ float2 mul(float2 a, float2 b) { return __ffma2_rn(a, b, kNegZero2); }
+  static __device__ __forceinline__ float2 div(float2 a, float2 b) {
+    return make_float2(__fdiv_rn(a.x, b.x), __fdiv_rn(a.y, b.y));
+  }
+};
+
 // Packed arithmetic of the fast collision (two cells per instruction).
 struct FastF32x2 {
   using T = float2;

@@ -12,12 +12,15 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "aux_kernels.cuh"
 #include "lbm_b200.h"
 #include "solver_internal.h"
 #include "step_kernel.cuh"
+#include "step_async.cuh"
+#include "step_ring.cuh"
 #include "step_tma.cuh"
 
 using namespace lbm_b200;
@@ -30,6 +33,7 @@ template <>
 struct Form<float> {
   using A = ExactF32;
   using Phys = ExactPhys<ExactF32>;
+  using PackedPhys = ExactPhysF32x2;
   static Phys::Consts consts(double tau, double fx, double fy) {
     return make_collide_consts<float>(float(tau), float(fx), float(fy));
   }
@@ -38,6 +42,7 @@ template <>
 struct Form<double> {
   using A = ExactF64;
   using Phys = ExactPhys<ExactF64>;
+  using PackedPhys = Phys;
   static Phys::Consts consts(double tau, double fx, double fy) {
     return make_collide_consts<double>(tau, fx, fy);
   }
@@ -46,6 +51,7 @@ template <>
 struct Form<__half> {
   using A = ExactF32;  // moment pass
   using Phys = FastPhys;
+  using PackedPhys = Phys;  // already packed
   static Phys::Consts consts(double tau, double fx, double fy) {
     return make_fast_consts(float(tau), float(fx), float(fy));
   }
@@ -54,6 +60,7 @@ template <>
 struct Form<__nv_bfloat16> {
   using A = ExactF32;
   using Phys = FastPhys;
+  using PackedPhys = Phys;  // already packed
   static Phys::Consts consts(double tau, double fx, double fy) {
     return make_fast_consts(float(tau), float(fx), float(fy));
   }
@@ -105,9 +112,13 @@ Eq9<typename StoreTraits<ST>::T> inlet_eq(const lbm_solver* s) {
   return host_equilibrium<T>(T(1), T(s->u_in), T(0));
 }
 
-template <class ST, bool kOpen, int kVariant>
+// Physics of a launch: the scalar form, or (kPacked) its two-cells-per-instruction twin.
+template <class ST, bool kPacked>
+using PhysOf = std::conditional_t<kPacked, typename Form<ST>::PackedPhys, typename Form<ST>::Phys>;
+
+template <class ST, bool kOpen, int kVariant, bool kPacked = false>
 int launch_steps_t(lbm_solver* s, int steps) {
-  using Phys = typename Form<ST>::Phys;
+  using Phys = PhysOf<ST, kPacked>;
   using T = typename StoreTraits<ST>::T;
   constexpr int G = StoreTraits<ST>::kVec;
   StepArgs<ST, Phys> a{};
@@ -140,9 +151,9 @@ int launch_steps_t(lbm_solver* s, int steps) {
 }
 
 // Warp-specialised bulk-copy step (step_tma.cuh) with kStages ring stages.
-template <class ST, bool kOpen, int kStages>
+template <class ST, bool kOpen, int kStages, bool kPacked = false>
 int launch_tma_t(lbm_solver* s, int steps) {
-  using Phys = typename Form<ST>::Phys;
+  using Phys = PhysOf<ST, kPacked>;
   using T = typename StoreTraits<ST>::T;
   using S = TmaShape<ST>;
   StepArgs<ST, Phys> a{};
@@ -177,14 +188,103 @@ int launch_tma_t(lbm_solver* s, int steps) {
   return LBM_OK;
 }
 
-// Automatic kernel choice (variant < 0): the warp-specialised ring (4) when the rows hold whole
-// 1024-cell-class tiles and there are enough tiles to fill the GPU, the direct kernel (0)
-// otherwise (narrow or small grids, where most consumer warps of a tile would idle).
+// Per-warp asynchronous-copy pipeline (step_async.cuh), kDepth chunks per warp, 4 warps per block.
+template <class ST, bool kOpen, int kDepth, bool kPacked = true>
+int launch_async_t(lbm_solver* s, int steps) {
+  using Phys = PhysOf<ST, kPacked>;
+  using T = typename StoreTraits<ST>::T;
+  constexpr int G = StoreTraits<ST>::kVec;
+  constexpr int kBlock = 128;
+  StepArgs<ST, Phys> a{};
+  a.mask = s->mask_d;
+  a.g = s->g;
+  a.cpr = (s->nx + 32 * G - 1) / (32 * G);
+  a.items = s->ny * a.cpr;
+  a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
+  const Eq9<T> e = inlet_eq<ST>(s);
+  for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
+  a.sc = s->sc;
+  const auto kernel = pull_step_async_kernel<ST, Phys, kOpen, kDepth>;
+  const size_t smem = async_smem_bytes<ST>(kDepth, kBlock / 32);
+  LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                   static_cast<int>(smem)));
+  int grid = s->grid;
+  if (grid <= 0) {
+    int per_sm = 0;
+    LBM_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kBlock, smem));
+    const int need = (a.items + kBlock / 32 - 1) / (kBlock / 32);
+    grid = std::max(1, std::min(need, std::max(1, per_sm) * s->sm_count));
+  }
+  s->last_grid = grid;
+  for (int k = 0; k < steps; ++k) {
+    a.src = static_cast<const ST*>(s->buf[s->cur]);
+    a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+    kernel<<<grid, kBlock, smem, s->stream>>>(a);
+    s->cur ^= 1;
+  }
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+// Warp-specialised ring with one cell per lane (step_ring.cuh); plain FP32 / FP64 storage only
+// (the 16-bit forms run the bulk-copy kernel of variant 4 instead).
+template <class ST, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
+int launch_ring_t(lbm_solver* s, int steps) {
+  if constexpr (!std::is_same<ST, float>::value && !std::is_same<ST, double>::value) {
+    return launch_tma_t<ST, kOpen, 2>(s, steps);
+  } else {
+    using A = typename Form<ST>::A;
+    using Phys = ExactPhys<A>;
+    using T = typename StoreTraits<ST>::T;
+    using S = RingShape<ST, kW, kC>;
+    StepArgs<ST, Phys> a{};
+    a.mask = s->mask_d;
+    a.g = s->g;
+    a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
+    const Eq9<T> e = inlet_eq<ST>(s);
+    for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
+    a.sc = s->sc;
+    const int tpr = (s->nx + S::TW - 1) / S::TW;
+    const int tiles = tpr * s->ny;
+    const auto kernel = pull_step_ring_kernel<ST, A, kOpen, kW, kC, kStages, kMinBlocks>;
+    const size_t smem = ring_smem_bytes<S>(kStages);
+    LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     static_cast<int>(smem)));
+    int grid = s->grid;
+    if (grid <= 0) {
+      int per_sm = 0;
+      LBM_CUDA(s, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, S::kThreads, smem));
+      grid = std::max(1, std::min(tiles, std::max(1, per_sm) * s->sm_count));
+    }
+    s->last_grid = grid;
+    for (int k = 0; k < steps; ++k) {
+      a.src = static_cast<const ST*>(s->buf[s->cur]);
+      a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+      kernel<<<grid, S::kThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
+      s->cur ^= 1;
+    }
+    LBM_CUDA(s, cudaGetLastError());
+    return LBM_OK;
+  }
+}
+
+constexpr int kMaskPadWords = 80;
+
+// Automatic kernel choice (variant < 0). Plain FP32 / FP64: the one-cell-per-lane ring (12) when
+// there are at least two tiles per SM, the direct kernel (0) otherwise. 16-bit forms: the
+// bulk-copy kernel (4) when the rows hold whole tiles and there are enough tiles to fill the GPU,
+// the direct kernel otherwise (narrow or small grids, where most consumer warps would idle).
 template <class ST>
 int auto_variant(const lbm_solver* s) {
-  using S = TmaShape<ST>;
-  const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
-  return (s->nx >= S::TW && tiles >= 4LL * s->sm_count) ? 4 : 0;
+  if constexpr (std::is_same<ST, float>::value || std::is_same<ST, double>::value) {
+    using S = RingShape<ST, 8, 2>;
+    const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
+    return tiles >= 2LL * s->sm_count ? 12 : 0;
+  } else {
+    using S = TmaShape<ST>;
+    const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
+    return (s->nx >= S::TW && tiles >= 4LL * s->sm_count) ? 4 : 0;
+  }
 }
 
 template <class ST, bool kOpen>
@@ -197,6 +297,16 @@ int launch_steps_o(lbm_solver* s, int steps) {
     case 4: return launch_tma_t<ST, kOpen, 2>(s, steps);
     case 5: return launch_tma_t<ST, kOpen, 3>(s, steps);
     case 6: return launch_tma_t<ST, kOpen, 4>(s, steps);
+    case 7: return launch_tma_t<ST, kOpen, 2, true>(s, steps);
+    case 8: return launch_steps_t<ST, kOpen, 0, true>(s, steps);
+    case 9: return launch_async_t<ST, kOpen, 2>(s, steps);
+    case 10: return launch_async_t<ST, kOpen, 3>(s, steps);
+    case 11: return launch_async_t<ST, kOpen, 4>(s, steps);
+    case 12: return launch_ring_t<ST, kOpen, 8, 2, 2, 1>(s, steps);
+    case 13: return launch_ring_t<ST, kOpen, 8, 2, 3, 1>(s, steps);
+    case 14: return launch_ring_t<ST, kOpen, 8, 2, 2, 4>(s, steps);
+    case 15: return launch_ring_t<ST, kOpen, 4, 2, 3, 1>(s, steps);
+    case 16: return launch_ring_t<ST, kOpen, 4, 2, 3, 7>(s, steps);
     default: return launch_steps_t<ST, kOpen, 0>(s, steps);
   }
 }
@@ -399,16 +509,14 @@ int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, doub
 
   const int per_line = 128 / elem;
   const int pitch = (nx + per_line - 1) / per_line * per_line;
-  // Mask rows cover whole tiles of the widest kernel (a warp-specialised tile is kConsumers
-  // chunks of 32 * vec cells) plus the 4 words its bulk copy of a tile's mask row reads past the
-  // tile; lanes past the row end read their (all-solid) window. The word count is a multiple of
-  // 4 so that every row starts on a 16-byte boundary (bulk-copy alignment).
-  const int span = kConsumers * 32 * s->vec;
-  const int tiles_per_row = (nx + span - 1) / span;
+  // Mask rows extend kMaskPadWords words (all solid) past the row: a staged copy of a tile's
+  // mask words reads up to the tile width / 32 + 4 words (at most 68) from the tile's first word,
+  // and lanes past the row end read their (all-solid) window. The word count is a multiple of 4
+  // so that every row starts on a 16-byte boundary (asynchronous-copy alignment).
   s->g.nx = nx;
   s->g.ny = ny;
   s->g.pitch = pitch;
-  s->g.mask_words = tiles_per_row * span / 32 + 4;
+  s->g.mask_words = ((nx + 31) / 32 + kMaskPadWords + 3) / 4 * 4;
   s->g.plane = static_cast<long long>(pitch) * ny;
   s->g.open_x = 0;
 
@@ -683,8 +791,8 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
 
 int lbm_set_variant(lbm_solver* s, int variant) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
-  if (variant < -1 || variant >= kStepVariants + 3)
-    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 7)");
+  if (variant < -1 || variant > 16)
+    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 16]");
   s->variant = variant;
   return LBM_OK;
 }

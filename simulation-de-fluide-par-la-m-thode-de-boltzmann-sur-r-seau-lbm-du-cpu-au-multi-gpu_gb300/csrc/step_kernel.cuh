@@ -57,6 +57,41 @@ struct ExactPhys {
   }
 };
 
+// Exact FP32 physics, two cells per packed instruction: the same correctly rounded operations
+// per cell as ExactPhys<ExactF32>, so the same bits.
+struct ExactPhysF32x2 {
+  using T = float;
+  using Consts = CollideConsts<float>;
+  template <int G>
+  static __device__ __forceinline__ void collide_all(const float (&v)[kQ][G], const Consts& k,
+                                                     float (&out)[kQ][G]) {
+    static_assert(G % 2 == 0, "cells are collided in pairs");
+    CollideConsts<float2> k2;
+    k2.omega = make_float2(k.omega, k.omega);
+    k2.force_prefactor = make_float2(k.force_prefactor, k.force_prefactor);
+    k2.fx = make_float2(k.fx, k.fx);
+    k2.fy = make_float2(k.fy, k.fy);
+    k2.hfx = make_float2(k.hfx, k.hfx);
+    k2.hfy = make_float2(k.hfy, k.hfy);
+    k2.cf_x = make_float2(k.cf_x, k.cf_x);
+    k2.cf_y = make_float2(k.cf_y, k.cf_y);
+    k2.cf_p = make_float2(k.cf_p, k.cf_p);
+    k2.cf_q = make_float2(k.cf_q, k.cf_q);
+#pragma unroll
+    for (int c = 0; c < G; c += 2) {
+      float2 g[kQ], o[kQ];
+#pragma unroll
+      for (int i = 0; i < kQ; ++i) g[i] = make_float2(v[i][c], v[i][c + 1]);
+      collide_exact<ExactF32x2>(g, k2, o);
+#pragma unroll
+      for (int i = 0; i < kQ; ++i) {
+        out[i][c] = o[i].x;
+        out[i][c + 1] = o[i].y;
+      }
+    }
+  }
+};
+
 // FP32 physics of the 16-bit storage forms (FMA, one reciprocal; not bit-exact), two cells per
 // packed instruction.
 struct FastPhys {

@@ -1,0 +1,244 @@
+// Warp-specialised pull stream-collide step, one cell per lane (plain FP32 / FP64 storage).
+// Same results as pull_step_kernel (step_kernel.cuh); same producer as pull_step_tma_kernel
+// (step_tma.cuh), different consumers:
+//
+//   * a tile is TW = kW * 32 * kC consecutive cells of one row; the producer warp (one lane)
+//     streams, per tile, the 9 source plane rows (plus a 16-byte halo each side), the 3 mask rows
+//     and, on a periodic row's first and last tile, the 16-byte blocks holding the wrapped
+//     neighbours (cell nx - 1 of the 3 planes moving right, cell 0 of the 3 moving left) into a
+//     shared ring stage with cp.async.bulk, completing on the stage's "full" mbarrier;
+//   * consumer warp w owns the strip of 32 * kC cells tx0 + w * 32 kC .., and lane l the cells
+//     strip + 32 c + l (c = 0 .. kC - 1): consecutive lanes hold consecutive cells, so each
+//     plane value is one conflict-free shared load at offset -c_x, and each of the 9 results is
+//     one fully coalesced 32 * element-size warp store;
+//   * a lane keeps one cell live at a time (9 inputs, 9 outputs, the collision's temporaries),
+//     which leaves registers for many resident warps: the exact collision is a long chain of
+//     dependent IEEE operations, and warps are what hides its latency;
+//   * one vote per strip tells whether any of its cells or their neighbours is solid; only then
+//     are per-cell neighbour bits formed and bounce-back values read (opposite population of the
+//     cell itself, from global memory);
+//   * waits are bounded as in the bulk-copy kernel (error flag, LBM_ERR_TIMEOUT on the host).
+#pragma once
+
+#include "step_tma.cuh"
+
+namespace lbm_b200 {
+
+template <class ST, int kW, int kC>
+struct RingShape {
+  static constexpr int H = 16 / static_cast<int>(sizeof(ST));  // halo elements (16 bytes)
+  static constexpr int SW = 32 * kC;                            // strip width (cells per warp)
+  static constexpr int TW = kW * SW;                            // tile width
+  static constexpr int SROW = TW + 2 * H;
+  static constexpr int MW = TW / 32 + 4;  // staged mask words per row
+  static constexpr int kPlaneBytes = kQ * SROW * static_cast<int>(sizeof(ST));
+  static constexpr int kMaskBytes = 3 * MW * 4;
+  static constexpr int kWrapBytes = 6 * 16;
+  static constexpr int kStageBytes = kPlaneBytes + kMaskBytes + kWrapBytes;
+  static constexpr int kThreads = 32 * (kW + 1);
+  static_assert((TW / 32) % 4 == 0, "mask rows must stay 16-byte aligned");
+  static_assert(kStageBytes % 16 == 0, "stages must stay 16-byte aligned");
+};
+
+template <class S>
+constexpr size_t ring_smem_bytes(int stages) {
+  return static_cast<size_t>(stages) * S::kStageBytes + 2 * stages * sizeof(uint64_t);
+}
+
+// Directions whose wrapped source lies at the other end of the row: c_x = +1 (1, 5, 8) read
+// cell nx - 1 at x = 0, c_x = -1 (3, 6, 7) read cell 0 at x = nx - 1.
+__device__ __forceinline__ int wrap_dir(int j) {
+  return j == 0 ? 1 : j == 1 ? 5 : j == 2 ? 8 : j == 3 ? 3 : j == 4 ? 6 : 7;
+}
+
+// One cell of a strip. st: stage planes (plane i row at st + i * SROW, local column lx = cell x);
+// sm: 3 staged mask rows (y - 1, y, y + 1) whose word 0 is word tx0 / 32; wr: wrap blocks.
+template <class ST, class A, bool kOpen, class S>
+__device__ __forceinline__ void ring_cell(const StepArgs<ST, ExactPhys<A>>& p, const ST* st,
+                                          const uint32_t* sm, const ST* wr, int y, int ym, int yp,
+                                          int x, int lx, int word, int lane, bool solids) {
+  using T = typename A::T;
+  const int nx = p.g.nx;
+  const long long plane = p.g.plane;
+  T v[kQ];
+#pragma unroll
+  for (int i = 0; i < kQ; ++i) v[i] = st[i * S::SROW + lx - dir_cx(i)];
+  if (!kOpen) {
+    if (x == 0) {
+      const int k = (nx - 1) & (S::H - 1);
+      v[1] = wr[0 * S::H + k];
+      v[5] = wr[1 * S::H + k];
+      v[8] = wr[2 * S::H + k];
+    }
+    if (x == nx - 1) {
+      v[3] = wr[3 * S::H];
+      v[6] = wr[4 * S::H];
+      v[7] = wr[5 * S::H];
+    }
+  }
+  uint32_t nm = 0, n0 = 0, np = 0;  // bits 0, 1, 2: cells x - 1, x, x + 1 of rows y - 1, y, y + 1
+  if (solids) {
+    nm = __funnelshift_r(sm[word], sm[word + 1], lane) & 7u;
+    n0 = __funnelshift_r(sm[S::MW + word], sm[S::MW + word + 1], lane) & 7u;
+    np = __funnelshift_r(sm[2 * S::MW + word], sm[2 * S::MW + word + 1], lane) & 7u;
+    if (!(n0 & 2u) && (nm | n0 | np) != 0u) {
+#pragma unroll
+      for (int i = 1; i < kQ; ++i) {
+        const uint32_t w = dir_cy(i) == 1 ? nm : (dir_cy(i) == -1 ? np : n0);
+        if ((w >> (1 - dir_cx(i))) & 1u)
+          v[i] = __ldg(p.src + dir_opp(i) * plane + static_cast<long long>(y) * p.g.pitch + x);
+      }
+    }
+  }
+  if (kOpen) {
+    if (x == 0) {
+      v[1] = p.eq_in[1];
+      v[5] = p.eq_in[5];
+      v[8] = p.eq_in[8];
+    }
+    if (x == nx - 1) {
+#pragma unroll
+      for (int i = 1; i < kQ; ++i) {
+        if (dir_cx(i) != -1) continue;
+        // Zero-gradient outflow: the source is cell nx - 1 of row y - c_y; bounce-back from cell
+        // nx - 2 of row y when that source is solid.
+        const uint32_t w = dir_cy(i) == 1 ? nm : (dir_cy(i) == -1 ? np : n0);
+        v[i] = ((w >> 1) & 1u)
+                   ? __ldg(p.src + dir_opp(i) * plane + static_cast<long long>(y) * p.g.pitch + (nx - 2))
+                   : st[i * S::SROW + lx];
+      }
+    }
+  }
+  (void)ym;
+  (void)yp;
+  T out[kQ];
+  collide_exact<A>(v, p.k, out);
+  ST* d = p.dst + static_cast<long long>(y) * p.g.pitch + x;
+#pragma unroll
+  for (int i = 0; i < kQ; ++i) d[i * plane] = out[i];
+}
+
+template <class ST, class A, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
+__global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
+    pull_step_ring_kernel(const StepArgs<ST, ExactPhys<A>> p, int tiles_per_row, int tiles, int* err) {
+  using S = RingShape<ST, kW, kC>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);
+  uint64_t* empty = full + kStages;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nx = p.g.nx, ny = p.g.ny;
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < kStages; ++s) {
+      mbar_init(&full[s], 1);
+      mbar_init(&empty[s], kW);
+    }
+    mbar_fence_init();
+  }
+  __syncthreads();
+
+  if (warp == 0) {
+    if (lane != 0) return;
+    // Producer.
+    int s = 0, issued = 0;
+    uint32_t phase = 0;
+    bool ok = true;
+    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++issued) {
+      if (issued >= kStages && !mbar_wait_bounded(&empty[s], phase ^ 1u, err)) {
+        ok = false;
+        break;
+      }
+      const int y = tile / tiles_per_row;
+      const int tx0 = (tile - y * tiles_per_row) * S::TW;
+      const int ym = y == 0 ? ny - 1 : y - 1;
+      const int yp = y == ny - 1 ? 0 : y + 1;
+      const int xs = tx0 - S::H > 0 ? tx0 - S::H : 0;
+      const int xe = tx0 + S::TW + S::H < p.g.pitch ? tx0 + S::TW + S::H : p.g.pitch;
+      const uint32_t bytes = static_cast<uint32_t>((xe - xs) * sizeof(ST));
+      const bool wrap_lo = !kOpen && tx0 == 0;
+      const bool wrap_hi = !kOpen && tx0 + S::TW >= nx;
+      mbar_arrive_expect_tx(&full[s], kQ * bytes + S::kMaskBytes + (wrap_lo ? 48u : 0u) +
+                                          (wrap_hi ? 48u : 0u));
+      unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
+      ST* stage = reinterpret_cast<ST*>(base);
+#pragma unroll
+      for (int i = 0; i < kQ; ++i) {
+        const ST* src = p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xs;
+        bulk_copy_g2s(stage + i * S::SROW + (xs - (tx0 - S::H)), src, bytes, &full[s]);
+      }
+      uint32_t* smask = reinterpret_cast<uint32_t*>(base + S::kPlaneBytes);
+      const int r3[3] = {ym, y, yp};
+#pragma unroll
+      for (int r = 0; r < 3; ++r)
+        bulk_copy_g2s(smask + r * S::MW, p.mask + static_cast<size_t>(r3[r]) * p.g.mask_words + (tx0 >> 5),
+                      S::MW * 4, &full[s]);
+      ST* wr = reinterpret_cast<ST*>(base + S::kPlaneBytes + S::kMaskBytes);
+      if (wrap_lo) {
+        const int xb = (nx - 1) & ~(S::H - 1);
+        for (int j = 0; j < 3; ++j) {
+          const int i = wrap_dir(j);
+          bulk_copy_g2s(wr + j * S::H,
+                        p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xb, 16,
+                        &full[s]);
+        }
+      }
+      if (wrap_hi) {
+        for (int j = 3; j < 6; ++j) {
+          const int i = wrap_dir(j);
+          bulk_copy_g2s(wr + j * S::H,
+                        p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch, 16,
+                        &full[s]);
+        }
+      }
+      if (++s == kStages) {
+        s = 0;
+        phase ^= 1u;
+      }
+    }
+    if (!ok) {
+      for (int k = 0; k < kStages && k < issued; ++k) {
+        const int st = (s + kStages - 1 - k) % kStages;
+        const int use = (issued - 1 - k) / kStages;
+        mbar_wait_bounded(&full[st], static_cast<uint32_t>(use & 1), err);
+      }
+    }
+    return;
+  }
+
+  // Consumers.
+  const int cw = warp - 1;
+  int s = 0;
+  uint32_t phase = 0;
+  for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
+    if (!mbar_wait_bounded_warp(&full[s], phase, err)) return;
+    const int y = tile / tiles_per_row;
+    const int tx0 = (tile - y * tiles_per_row) * S::TW;
+    const int xw = tx0 + cw * S::SW;
+    if (xw < nx) {
+      const unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
+      const ST* st = reinterpret_cast<const ST*>(base);
+      const uint32_t* sm = reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes);
+      const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes);
+      const int ym = y == 0 ? ny - 1 : y - 1;
+      const int yp = y == ny - 1 ? 0 : y + 1;
+      const int w0 = cw * kC;  // first staged mask word of the strip
+      // Any solid among the strip's cells and their neighbours (words w0 .. w0 + kC of 3 rows).
+      uint32_t mine = 0;
+      if (lane < 3 * (kC + 1)) mine = sm[(lane / (kC + 1)) * S::MW + w0 + lane % (kC + 1)];
+      const bool solids = __any_sync(0xffffffffu, mine != 0u);
+#pragma unroll 1
+      for (int c = 0; c < kC; ++c) {
+        const int x = xw + 32 * c + lane;
+        if (x < nx)
+          ring_cell<ST, A, kOpen, S>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H, w0 + c, lane, solids);
+      }
+    }
+    __syncwarp();
+    if (lane == 0) mbar_arrive(&empty[s]);
+    if (++s == kStages) {
+      s = 0;
+      phase ^= 1u;
+    }
+  }
+}
+
+}  // namespace lbm_b200

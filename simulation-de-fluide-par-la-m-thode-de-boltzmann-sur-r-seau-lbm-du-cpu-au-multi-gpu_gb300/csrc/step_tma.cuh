@@ -151,33 +151,33 @@ __device__ __forceinline__ typename StoreTraits<ST>::T lds_one(const ST* p, int 
   return decode<ST>(*p, i, s);
 }
 
-// Mask window of cells x0 - 1 .. x0 + 30 from a staged mask row (word 0 = word tx0 / 32).
-__device__ __forceinline__ uint32_t smem_mask_window(const uint32_t* row, int x0, int tx0) {
-  const int w = (x0 - tx0) >> 5;
+// Mask window of cells x0 - 1 .. x0 + 30 from a staged mask row whose word 0 is word wb of the
+// row.
+__device__ __forceinline__ uint32_t smem_mask_window(const uint32_t* row, int x0, int wb) {
+  const int w = (x0 >> 5) - wb;
   return __funnelshift_r(row[w], row[w + 1], x0 & 31);
 }
 
-// Collides the consumer lane's G cells of one tile, reading the source planes from the shared
-// stage `st` (plane i at st + i * SROW, element 0 = column tx0 - H) and the mask rows y - 1, y,
-// y + 1 from `sm` (3 rows of MW words, word 0 = word tx0 / 32 of the row).
-template <class ST, class Phys, bool kOpen>
-__device__ __forceinline__ void tma_consume(const StepArgs<ST, Phys>& p, const ST* st,
-                                            const uint32_t* sm, int y, int tx0, int cw, int lane) {
+// Collides one lane's G cells x0 .. x0 + G - 1 of row y, reading the source planes from shared
+// memory (plane i row at st + i * kSrow, cell x0 at local column lx; the elements at lx - 1 and
+// lx + G hold cells x0 - 1 and x0 + G wherever those lie inside the row) and the mask rows
+// y - 1, y, y + 1 from `sm` (3 rows of kMw words, word 0 = word wb of the row). Every lane of the
+// warp calls it (warp-uniform skip of all-solid groups).
+template <class ST, class Phys, bool kOpen, int kSrow, int kMw>
+__device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const ST* st,
+                                              const uint32_t* sm, int wb, int y, int x0, int lx) {
   using T = typename StoreTraits<ST>::T;
-  using S = TmaShape<ST>;
-  constexpr int G = S::G;
+  constexpr int G = StoreTraits<ST>::kVec;
   constexpr uint32_t kFull = (1u << G) - 1u;
   const int nx = p.g.nx, ny = p.g.ny, pitch = p.g.pitch;
   const long long plane = p.g.plane;
-  const int x0 = tx0 + cw * 32 * G + lane * G;
   const bool active = x0 < nx;
-  const int lx = x0 - tx0 + S::H;  // local column of x0 in the stage
   const int ym = y == 0 ? ny - 1 : y - 1;
   const int yp = y == ny - 1 ? 0 : y + 1;
 
-  const uint32_t wm = smem_mask_window(sm, x0, tx0);
-  const uint32_t w0 = smem_mask_window(sm + S::MW, x0, tx0);
-  const uint32_t wp = smem_mask_window(sm + 2 * S::MW, x0, tx0);
+  const uint32_t wm = smem_mask_window(sm, x0, wb);
+  const uint32_t w0 = smem_mask_window(sm + kMw, x0, wb);
+  const uint32_t wp = smem_mask_window(sm + 2 * kMw, x0, wb);
   const int valid = nx - x0;
   uint32_t own = (w0 >> 1) & kFull;
   if (valid < G) own |= valid <= 0 ? kFull : (kFull & ~((1u << valid) - 1u));
@@ -187,7 +187,7 @@ __device__ __forceinline__ void tma_consume(const StepArgs<ST, Phys>& p, const S
   T v[kQ][G];
 #pragma unroll
   for (int i = 0; i < kQ; ++i) {
-    const ST* row = st + i * S::SROW;
+    const ST* row = st + i * kSrow;
     lds_vec<ST>(row + lx, v[i], i, p.sc);
     if (dir_cx(i) == 1) {
       // cell x0 + k reads x0 + k - 1
@@ -345,9 +345,10 @@ __global__ void __launch_bounds__(kTmaThreads, kStages <= 3 ? 2 : 1)
     const int y = tile / tiles_per_row;
     const int tx0 = (tile - y * tiles_per_row) * S::TW;
     const unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
-    tma_consume<ST, Phys, kOpen>(p, reinterpret_cast<const ST*>(base),
-                                 reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes), y, tx0,
-                                 cw, lane);
+    const int x0 = tx0 + cw * 32 * S::G + lane * S::G;
+    consume_cells<ST, Phys, kOpen, S::SROW, S::MW>(
+        p, reinterpret_cast<const ST*>(base), reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes),
+        tx0 >> 5, y, x0, x0 - tx0 + S::H);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
     if (++s == kStages) {
