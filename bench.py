@@ -200,6 +200,52 @@ def cpu_baseline(orc, n: int, budget_s: float = 8.0):
                       f"{threads} OpenMP threads"}
 
 
+def accuracy_report(pkg):
+    """Velocity L2 error and mass drift of the 16-bit forms against the FP64 form on the
+    cylinder-wake geometry (1024 x 256, disc D = 32, tau 0.548, uniform start u = (0.05, 0),
+    F = (1.5e-7, 0)) after 4000 steps."""
+    nx, ny, tau, fx, steps, init = 1024, 256, 0.548, 1.5e-7, 4000, (1.0, 0.05, 0.0)
+    mask = pkg.workloads.cylinder_wake(nx, ny)
+    out, ref = {}, None
+    for form in ("fp16", "bf16"):
+        r, ref = pkg.accuracy.compare_forms(pkg, nx, ny, mask, tau, fx, 0.0, steps, form,
+                                            init=init, reference=ref)
+        out[form] = {k: (float(f"{v:.4g}") if isinstance(v, float) else v) for k, v in r.items()
+                     if k != "form"}
+    out["workload"] = (f"cylinder wake {nx}x{ny}, disc D=32 at (256,129), tau {tau}, "
+                       f"F=({fx},0), start u=(0.05,0), {steps} steps, stochastic rounding")
+    return out
+
+
+def adjoint_report(pkg, peak):
+    """Adjoint form on its workload (512 x 128 channel, Brinkman field, J = mean u_x over the
+    last 100 of 2000 steps, checkpoints every 100 steps), a batch of 32 alpha fields in FP32:
+    forward and backward step times (recomputation included) and their ratio."""
+    nx, ny, tau, fx, steps, window, batch = 512, 128, 0.6, 5e-6, 2000, 100, 32
+    mask = pkg.workloads.adjoint_channel(nx, ny)
+    alpha = pkg.workloads.brinkman_field(nx, ny, seed=1234)
+    alpha[mask != 0] = 0.0
+    out = {}
+    for prec in ("fp32", "fp64"):
+        try:
+            with pkg.Adjoint(nx, ny, tau, fx, 0.0, mask, precision=prec, batch=batch,
+                             checkpoint_every=100) as a:
+                a.set_alpha(np.stack([alpha] * batch))
+                a.forward(steps, window)
+                a.backward()
+                f, b = a.step_times()
+            cells = nx * ny * batch
+            out[prec] = {"forward_step_us": round(f * 1e6, 2), "backward_step_us": round(b * 1e6, 2),
+                         "backward_over_forward": round(b / f, 3),
+                         "forward_mlups": round(cells / f / 1e6, 1),
+                         "backward_mlups": round(cells / b / 1e6, 1)}
+        except Exception as e:
+            out[prec] = {"error": str(e)[:200]}
+    out["workload"] = (f"channel {nx}x{ny}, tau {tau}, F=({fx},0), Brinkman alpha in [0,0.1], "
+                       f"{steps} steps, J window {window}, K=100, batch {batch}")
+    return out
+
+
 def run_ours(args):
     import torch
 
@@ -213,10 +259,14 @@ def run_ours(args):
         orc.build()
     n = args.nx
     warmup = max(args.warmup, 3)
+    prec = args.precision
     _, mask, s0 = channel_state(orc, n, "f32")
+    s_head = s0.astype(np.float64) if prec == "fp64" else s0
 
-    solver = pkg.Solver(n, n, TAU, FX, FY, mask, precision="fp32")
-    solver.set_populations(s0)
+    solver = pkg.Solver(n, n, TAU, FX, FY, mask, precision=prec)
+    if args.variant >= 0:
+        solver.set_variant(args.variant)
+    solver.set_populations(s_head)
     solver.run(warmup)
     sampler = ClockSampler(local)
     sampler.start()
@@ -238,16 +288,17 @@ def run_ours(args):
     value = cells * args.steps * world / secs / 1e6
     step_s = secs / args.steps
     peak, peak_kind = measured_peak()
-    achieved = BYTES_PER_CELL["fp32"] * cells / step_s / 1e9
-    traffic = profiled_traffic("fp32", n)
+    achieved = BYTES_PER_CELL[prec] * cells / step_s / 1e9
+    traffic = profiled_traffic(prec, n)
 
     # e2e through the public API: pinned host input, 1000 steps, host output.
     e2e = None
     if args.e2e_jobs > 0:
-        pin = torch.empty(s0.size, dtype=torch.float32).pin_memory()
-        pin.numpy()[:] = s0
-        outs = [torch.empty(cells, dtype=torch.float32).pin_memory() for _ in range(3)]
-        with pkg.Solver(n, n, TAU, FX, FY, mask, precision="fp32") as s:
+        tdt = torch.float64 if prec == "fp64" else torch.float32
+        pin = torch.empty(s0.size, dtype=tdt).pin_memory()
+        pin.numpy()[:] = s_head
+        outs = [torch.empty(cells, dtype=tdt).pin_memory() for _ in range(3)]
+        with pkg.Solver(n, n, TAU, FX, FY, mask, precision=prec) as s:
             s.set_populations(pin.numpy())
             s.run(10)
             s.macroscopic([o.numpy() for o in outs])
@@ -262,27 +313,34 @@ def run_ours(args):
             barrier(dist)
             dt = max_over_ranks(time.perf_counter() - t0, dist)
         e2e = {"value": cells * E2E_LATTICE_STEPS * args.e2e_jobs * world / dt / 1e6,
-               "unit": "MLUPS", "h2d_bytes_per_step": int(s0.nbytes),
-               "d2h_bytes_per_step": int(3 * cells * 4),
+               "unit": "MLUPS", "h2d_bytes_per_step": int(s_head.nbytes),
+               "d2h_bytes_per_step": int(3 * cells * s_head.itemsize),
                "lattice_steps_per_e2e_step": E2E_LATTICE_STEPS, "e2e_steps": args.e2e_jobs,
                "api": "lbm_set_populations + lbm_run(1000) + lbm_macroscopic (C ABI)"}
 
     forms = {}
     if args.forms and rank == 0:
-        for prec, steps in (("fp16", 400), ("bf16", 400), ("fp64", 100)):
+        for fp, steps in (("fp32", 2000), ("fp16", 2000), ("bf16", 2000), ("fp64", 100)):
+            if fp == prec:
+                forms[fp] = {"mlups": round(value / world, 1), "bytes_per_cell": BYTES_PER_CELL[fp],
+                             "achieved_gbs": round(achieved, 1),
+                             "hbm_frac": round(achieved / peak, 4), "steps": args.steps}
+                continue
             try:
-                st = s0.astype(np.float64) if prec == "fp64" else s0
-                ml, _ = time_form(pkg, mask, st, n, prec, steps, 20)
-                gbs = BYTES_PER_CELL[prec] * ml * 1e6 / 1e9
-                forms[prec] = {"mlups": round(ml, 1), "bytes_per_cell": BYTES_PER_CELL[prec],
-                               "achieved_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
-                               "steps": steps}
+                st = s0.astype(np.float64) if fp == "fp64" else s0
+                ml, _ = time_form(pkg, mask, st, n, fp, steps, 20)
+                gbs = BYTES_PER_CELL[fp] * ml * 1e6 / 1e9
+                forms[fp] = {"mlups": round(ml, 1), "bytes_per_cell": BYTES_PER_CELL[fp],
+                             "achieved_gbs": round(gbs, 1), "hbm_frac": round(gbs / peak, 4),
+                             "steps": steps}
             except Exception as e:  # a form that fails is reported, not hidden
-                forms[prec] = {"error": str(e)[:200]}
-        forms["fp32"] = {"mlups": round(value / world, 1), "bytes_per_cell": 72,
-                         "achieved_gbs": round(achieved, 1), "hbm_frac": round(achieved / peak, 4)}
-        if "mlups" in forms.get("fp16", {}):
+                forms[fp] = {"error": str(e)[:200]}
+        if "mlups" in forms.get("fp16", {}) and "mlups" in forms.get("fp32", {}):
             forms["fp16_over_fp32"] = round(forms["fp16"]["mlups"] / forms["fp32"]["mlups"], 3)
+        if args.accuracy:
+            forms["accuracy_vs_fp64"] = accuracy_report(pkg)
+        if args.adjoint:
+            forms["adjoint"] = adjoint_report(pkg, peak)
 
     cpu = None
     if rank == 0 and args.cpu_baseline:
@@ -293,16 +351,20 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "MLUPS", "n_gpus": world,
         "steps": args.steps, "warmup": warmup, "ms_per_step": round(step_s * 1e3, 5),
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32", "fp64": "f64", "fp16": "f32 (f16 storage)",
+                  "bf16": "f32 (bf16 storage)"}[prec],
         "data": "synthetic: seeded SplitMix64 perturbation of f_i - w_i in [-1e-4, 1e-4]",
         "config": {"workload": f"walled channel {n}x{n}, periodic x, tau 0.6, F=(1e-6,0), "
-                               "plain FP32 pull stream-collide (bit-exact with reference v0)",
-                   "nx": n, "ny": n, "form": "fp32", "parallelism": f"replicas x{world}",
+                               + ("plain FP32 pull stream-collide (bit-exact with reference v0)"
+                                  if prec == "fp32" else f"{prec} form of the pull stream-collide"),
+                   "nx": n, "ny": n, "form": prec, "variant": args.variant,
+                   "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (population buffer 604 MB > 129 MB), no flush"},
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak,
                      "unit": "GB/s", "frac": round(achieved / peak, 4),
                      "traffic": traffic, "peak_kind": peak_kind,
-                     "algorithmic_bytes_per_launch": BYTES_PER_CELL["fp32"] * cells},
+                     "algorithmic_bytes_per_launch": BYTES_PER_CELL[prec] * cells},
         "clocks": sampler.summary(),
         "gpu_launches": args.steps,
         "e2e": e2e,
@@ -380,6 +442,14 @@ def main():
     ap.add_argument("--e2e-jobs", type=int, default=3)
     ap.add_argument("--no-forms", dest="forms", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
+    ap.add_argument("--precision", choices=["fp32", "fp64", "fp16", "bf16"], default="fp32",
+                    help="form of the headline (timed) run; the default is the reference's FP32")
+    ap.add_argument("--variant", type=int, default=-1,
+                    help="step-kernel variant of the headline run (-1: automatic choice)")
+    ap.add_argument("--no-accuracy", dest="accuracy", action="store_false",
+                    help="skip the 16-bit forms' accuracy runs against FP64")
+    ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
+                    help="skip the adjoint form")
     args = ap.parse_args()
     if args.steps < 1:
         ap.error("--steps must be >= 1")

@@ -45,7 +45,13 @@ enum {
 };
 
 /* Storage / arithmetic forms. FP32 and FP64 are bit-exact with the reference's v0 in float and
- * double. FP16_STORE / BF16_STORE keep g_i * scale_i in 16 bits and compute in FP32. */
+ * double. FP16_STORE / BF16_STORE keep g_i * scale_i in 16 bits (scale_i a power of two per
+ * plane) and compute in FP32. The step kernels round each stored value stochastically (unbiased:
+ * the expected stored value is the FP32 result), with random bits that are a fixed function of
+ * (cell, plane, lattice step), so a run is reproducible; round-to-nearest would drop the sub-ulp
+ * per-step increments of low-Mach flows. Uploads (lbm_set_populations, lbm_init_equilibrium)
+ * round to nearest. A value beyond the format's range saturates, and lbm_check_finite reports a
+ * saturated value as non-finite. */
 typedef enum {
   LBM_FP32 = 0,
   LBM_FP64 = 1,
@@ -146,14 +152,16 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * eight consumer warps collide from shared memory. 7 and 8: variants 4 and 0 with the FP32
  * collision computed for two cells per packed instruction (other precisions: same as 4 and 0).
  * 9, 10, 11: per-warp pipeline, each warp keeps 2, 3, 4 chunks in flight in its own
- * shared-memory ring with 16-byte asynchronous copies (packed FP32 collision). 12..16: producer
- * warp and bulk-copy ring as in 4, consumers with one cell per lane and consecutive lanes on
- * consecutive cells (plain FP32 / FP64 storage; the 16-bit forms run 4): 12 = 8 consumer warps x
- * 64-cell strips, 2 stages; 13 = the same with 3 stages; 14 = 12 capped at 56 registers for 4
- * resident blocks; 15 = 4 consumer warps, 3 stages; 16 = 15 capped for 7 resident blocks.
- * -1 (the default): plain FP32 / FP64 run 12 when there are at least two of its 512-cell
- * (FP64: 512-cell) tiles per SM, 0 otherwise; the 16-bit forms run 4 when the rows hold whole
- * tiles and there are enough tiles to fill the GPU, 0 otherwise. */
+ * shared-memory ring with 16-byte asynchronous copies (packed FP32 collision). 12..17: producer
+ * warp and bulk-copy ring as in 4, consumers with one cell (FP32 / FP64) or one pair of cells
+ * (16-bit storage) per lane, consecutive lanes on consecutive cells: 12 = 8 consumer warps,
+ * 2 passes per strip, 2 stages; 13 = the same with 3 stages; 14 = 12 capped at 56 registers for
+ * 4 resident blocks; 15 = 4 consumer warps, 3 stages; 16 = 15 capped for 7 resident blocks;
+ * 17 = 12 capped for 3 resident blocks.
+ * -1 (the default): 12 (plain FP32 / FP64, 512-cell tiles) or 17 (16-bit storage, 1024-cell
+ * tiles) when there are at least two tiles per SM, 0 otherwise.
+ * The 16-bit forms round stored populations stochastically (see lbm_create); every variant
+ * derives the same random bits, so the variants give the same results. */
 int lbm_set_variant(lbm_solver* s, int variant);
 
 /* Device memory of the two population buffers (for zero-copy consumers): plane stride and row

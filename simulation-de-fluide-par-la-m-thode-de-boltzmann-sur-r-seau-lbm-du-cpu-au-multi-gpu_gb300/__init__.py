@@ -17,7 +17,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import geometry, workloads  # noqa: F401  (re-exported)
+from . import accuracy, geometry, workloads  # noqa: F401  (re-exported)
 from .geometry import make_channel, make_cylinder, poiseuille_force  # noqa: F401
 
 _HERE = Path(__file__).resolve().parent

@@ -189,8 +189,8 @@ __global__ void finite_kernel(const ST* __restrict__ R, const uint32_t* __restri
     bool bad = false;
 #pragma unroll
     for (int i = 0; i < kQ; ++i) {
-      const double v = static_cast<double>(load_one<ST>(R + i * g.plane + cell_index(g, x, y), i, sc));
-      bad |= !isfinite(v);
+      const ST raw = R[i * g.plane + cell_index(g, x, y)];
+      bad |= !isfinite(static_cast<double>(decode<ST>(raw, i, sc))) || stored_saturated<ST>(raw);
     }
     if (bad) atomicExch(flag, 1);
   }

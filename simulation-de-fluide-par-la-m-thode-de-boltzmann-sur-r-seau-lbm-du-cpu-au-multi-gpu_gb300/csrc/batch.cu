@@ -54,7 +54,13 @@ struct BatchArgs {
   int count;
   int items;
   PlaneScales sc;
+  const uint32_t* step;  // lattice steps taken (device counter; stochastic-rounding key)
 };
+
+// Device step counter of a batch: read by every step launch, advanced by one after it (inside a
+// captured graph as well, so every replay of the graph rounds with fresh keys).
+__global__ void step_counter_add(uint32_t* c) { *c += 1u; }
+__global__ void step_counter_set(uint32_t* c, uint32_t v) { *c = v; }
 
 template <class ST, class Phys, int G>
 __global__ void __launch_bounds__(kBatchThreads)
@@ -63,6 +69,7 @@ __global__ void __launch_bounds__(kBatchThreads)
   __shared__ int s_item0[kBatchMaxInstances];
   for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_item0[k] = a.inst[k].item0;
   __syncthreads();
+  const uint32_t rkey = sr_step_key(*a.step);
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < a.items; item += nwarps) {
@@ -84,6 +91,8 @@ __global__ void __launch_bounds__(kBatchThreads)
     p.items = d.cpr * d.g.ny;
     p.k = d.k;
     p.sc = a.sc;
+    p.rkey = rkey;
+    p.key_base = d.off / kQ;
     const Chunk c = chunk_at<G>(item - d.item0, d.cpr, d.g.nx, d.g.ny, lane);
     T v[kQ][G];
     load_planes<ST, Phys, G>(p, c, v);
@@ -111,14 +120,14 @@ template <>
 struct BForm<__half> {
   using Phys = FastPhys;
   static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_fast_consts(float(tau), float(fx), float(fy));
+    return make_fast_consts(float(tau), float(fx), float(fy), kStoreScale16);
   }
 };
 template <>
 struct BForm<__nv_bfloat16> {
   using Phys = FastPhys;
   static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_fast_consts(float(tau), float(fx), float(fy));
+    return make_fast_consts(float(tau), float(fx), float(fy), kStoreScale16);
   }
 };
 
@@ -150,6 +159,8 @@ struct lbm_batch {
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaGraphExec_t graph = nullptr;
   int graph_cur = -1;  // buffer parity the graph was captured from
+  uint32_t t = 0;             // lattice steps taken (host copy of *step_d)
+  uint32_t* step_d = nullptr;  // device step counter
   int sm_count = 0, device = 0;
   std::string err, tune_report;
 };
@@ -224,10 +235,13 @@ int launch_batch_t(lbm_batch* b, int steps, bool prepare_only) {
   a.count = b->count;
   a.items = b->items;
   a.sc = b->sc;
+  a.step = b->step_d;
   for (int s = 0; s < steps; ++s) {
     a.src = static_cast<const ST*>(b->buf[b->cur]);
     a.dst = static_cast<ST*>(b->buf[b->cur ^ 1]);
     kernel<<<b->grid_eff, b->block, 0, b->stream>>>(a);
+    step_counter_add<<<1, 1, 0, b->stream>>>(b->step_d);
+    ++b->t;
     b->cur ^= 1;
   }
   const cudaError_t e = cudaPeekAtLastError();
@@ -307,6 +321,7 @@ int separate_t(lbm_batch* b, int steps) {
     a.items = a.cpr * in.ny;
     a.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
     a.sc = b->sc;
+    a.key_base = in.off / kQ;
     grids[k] = std::max(1, std::min((a.items + kStepThreads / 32 - 1) / (kStepThreads / 32),
                                     std::max(1, per_sm) * b->sm_count));
   }
@@ -316,8 +331,11 @@ int separate_t(lbm_batch* b, int steps) {
     for (int k = 0; k < b->count; ++k) {
       args[k].src = src + b->inst[k].off;
       args[k].dst = dst + b->inst[k].off;
+      args[k].rkey = sr_step_key(b->t);
       kernel<<<grids[k], kStepThreads, 0, b->stream>>>(args[k]);
     }
+    step_counter_add<<<1, 1, 0, b->stream>>>(b->step_d);
+    ++b->t;
     b->cur ^= 1;
   }
   B_CUDA(b, cudaGetLastError());
@@ -467,10 +485,10 @@ int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* con
   b->host_elem = precision == LBM_FP64 ? 8 : 4;
   b->count = count;
   b->inst.resize(count);
+  const bool s16 = precision == LBM_FP16_STORE || precision == LBM_BF16_STORE;
   for (int i = 0; i < kQ; ++i) {
-    const int e = (precision == LBM_FP16_STORE || precision == LBM_BF16_STORE) ? (i == 0 ? 15 : (i <= 4 ? 17 : 18)) : 0;
-    b->sc.enc[i] = std::ldexp(1.0f, e);
-    b->sc.dec[i] = std::ldexp(1.0f, -e);
+    b->sc.enc[i] = s16 ? kStoreScale16 : 1.0f;
+    b->sc.dec[i] = s16 ? 1.0f / kStoreScale16 : 1.0f;
   }
   auto fail = [&](int code) {
     lbm_batch_destroy(b);
@@ -522,6 +540,8 @@ int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* con
     e = cudaMemcpy(b->mask_d, all_words.data(), all_words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
   b->red_blocks = 4 * b->sm_count;
   if (e == cudaSuccess) e = cudaMalloc(&b->red, (b->red_blocks + 2) * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&b->step_d, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(b->step_d, 0, sizeof(uint32_t));
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
   *out = b;
   return LBM_OK;
@@ -532,7 +552,7 @@ int lbm_batch_destroy(lbm_batch* b) {
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
   for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->stage,
-                  static_cast<void*>(b->red)})
+                  static_cast<void*>(b->red), static_cast<void*>(b->step_d)})
     cudaFree(p);
   for (cudaEvent_t ev : b->ev)
     if (ev) cudaEventDestroy(ev);
@@ -643,8 +663,9 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
       }
     }
   }
-  // Time every candidate on the current state; the state advances, which is harmless for
-  // timing and is restored below by re-running the same number of steps from a saved copy.
+  // Time every candidate on the current state; the state and the step counter advance, which
+  // is harmless for timing, and both are put back from a saved copy afterwards.
+  const uint32_t t_saved = b->t;
   const size_t bytes = static_cast<size_t>(b->total_elems) * b->elem + 256;
   void* saved = nullptr;
   B_CUDA(b, cudaMalloc(&saved, bytes));
@@ -686,6 +707,8 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
     }
   }
   B_CUDA(b, cudaMemcpyAsync(b->buf[b->cur], saved, bytes, cudaMemcpyDeviceToDevice, b->stream));
+  step_counter_set<<<1, 1, 0, b->stream>>>(b->step_d, t_saved);
+  b->t = t_saved;
   B_CUDA(b, cudaStreamSynchronize(b->stream));
   cudaFree(saved);
   if (int rc = lbm_batch_set_launch(b, pick.G, pick.blk, pick.per_sm * b->sm_count)) return rc;

@@ -207,33 +207,46 @@ LBM_HD void moments_exact(const typename A::T (&g)[kQ], typename A::T hfx, typen
 // ---------------------------------------------------------------------------------------------
 // Fast FP32 collision of the 16-bit storage forms (not bit-exact; FMA, one reciprocal).
 //
-// omega g_eq_i + fp guo_i (fp = 1 - omega/2) regrouped per direction as
-//   w_i [ A + 3 fp cf_i + cu_i (B + 9 fp cf_i + C cu_i) ],
-//   A = omega drho - 1.5 omega rho |u|^2 - 3 fp (u.F),  B = 3 omega rho,  C = 4.5 omega rho,
-// which is the same polynomial as the reference's geq/guo (d2q9.hpp:40-50) with
-// (c_i - u).F = cf_i - u.F; out_i = (1 - omega) g_i + that.
+// Works on scaled populations G_i = S g_i (S a power of two, the storage scale of every plane)
+// and returns scaled results, so that no per-value rescaling is spent on loads and stores:
+// power-of-two scaling commutes with rounding, m = sum G_i / S and u = (m_x' + S F_x / 2) *
+// (1 / (S rho)) are the unscaled moments exactly, and S w_i folds into the per-direction
+// constants. The post-collision value omega g_eq_i + fp guo_i (fp = 1 - omega/2) is the
+// reference's geq/guo polynomial (d2q9.hpp:40-50) regrouped per pair of opposite directions
+// (c_j = -c_i, so cu_j = -cu_i, cf_j = -cf_i, w_j = w_i):
+//   S w_i t_i = E + N + O,  S w_j t_j = E + N - O,
+//   E = S w (a + c cu^2),  N = S w 9 fp cf_i cu,  O = S w (b cu + 3 fp cf_i),
+//   a = omega drho - 1.5 omega rho |u|^2 - 3 fp (u.F),  b = 3 omega rho,  c = 4.5 omega rho,
+// using (c_i - u).F = cf_i - u.F; out_i = (1 - omega) G_i + S w_i t_i.
 // ---------------------------------------------------------------------------------------------
 struct FastConsts {
   float omega, one_minus_omega;
-  float hfx, hfy;      // F / 2
+  float inv_scale;     // 1 / S
+  float shfx, shfy;    // S F / 2
   float fp3fx, fp3fy;  // 3 fp F
-  float k3[kQ];        // 3 fp cf_i
-  float k9[kQ];        // 9 fp cf_i
+  float w0, wax, wdg;  // S w_0, S w_axis, S w_diagonal
+  float wk3[kQ];       // S w_i 3 fp cf_i
+  float wk9[kQ];       // S w_i 9 fp cf_i
 };
 
-inline FastConsts make_fast_consts(float tau, float fx, float fy) {
+inline FastConsts make_fast_consts(float tau, float fx, float fy, float scale = 1.0f) {
   FastConsts c{};
   c.omega = 1.0f / tau;
   c.one_minus_omega = 1.0f - c.omega;
   const float fp = 1.0f - 0.5f * c.omega;
-  c.hfx = 0.5f * fx;
-  c.hfy = 0.5f * fy;
+  c.inv_scale = 1.0f / scale;
+  c.shfx = scale * (0.5f * fx);
+  c.shfy = scale * (0.5f * fy);
   c.fp3fx = 3.0f * fp * fx;
   c.fp3fy = 3.0f * fp * fy;
+  c.w0 = scale * weight<float>(0);
+  c.wax = scale * weight<float>(1);
+  c.wdg = scale * weight<float>(5);
   for (int i = 0; i < kQ; ++i) {
     const float cf = static_cast<float>(dir_cx(i)) * fx + static_cast<float>(dir_cy(i)) * fy;
-    c.k3[i] = 3.0f * fp * cf;
-    c.k9[i] = 9.0f * fp * cf;
+    const float w = scale * weight<float>(i);
+    c.wk3[i] = w * (3.0f * fp * cf);
+    c.wk9[i] = w * (9.0f * fp * cf);
   }
   return c;
 }
@@ -262,34 +275,45 @@ struct FastF32 {
   }
 };
 
+// Outputs of one pair of opposite directions i (cu) and j (-cu) of weight class (wa, wb, wc).
+template <class P>
+LBM_HD void fast_pair(const typename P::T (&g)[kQ], const FastConsts& kc, int i, int j,
+                      typename P::T cu, typename P::T wa, typename P::T wb, typename P::T wc,
+                      typename P::T om1, typename P::T (&out)[kQ]) {
+  using T = typename P::T;
+  const T e = P::fma(P::mul(wc, cu), cu, wa);
+  const T o = P::fma(wb, cu, P::k(kc.wk3[i]));
+  const T en = P::fma(P::k(kc.wk9[i]), cu, e);
+  out[i] = P::fma(om1, g[i], P::add(en, o));
+  out[j] = P::fma(om1, g[j], P::sub(en, o));
+}
+
 template <class P>
 LBM_HD void collide_fast_t(const typename P::T (&g)[kQ], const FastConsts& kc,
                            typename P::T (&out)[kQ]) {
   using T = typename P::T;
-  const T m0 = P::add(P::add(P::add(P::add(g[0], g[1]), P::add(g[2], g[3])),
-                             P::add(P::add(g[4], g[5]), P::add(g[6], g[7]))), g[8]);
-  const T mx = P::add(P::add(P::sub(g[1], g[3]), P::sub(g[5], g[6])), P::sub(g[8], g[7]));
-  const T my = P::sub(P::add(P::sub(g[2], g[4]), P::add(g[5], g[6])), P::add(g[7], g[8]));
+  const T m0s = P::add(P::add(P::add(P::add(g[0], g[1]), P::add(g[2], g[3])),
+                              P::add(P::add(g[4], g[5]), P::add(g[6], g[7]))), g[8]);
+  const T mxs = P::add(P::add(P::sub(g[1], g[3]), P::sub(g[5], g[6])), P::sub(g[8], g[7]));
+  const T mys = P::sub(P::add(P::sub(g[2], g[4]), P::add(g[5], g[6])), P::add(g[7], g[8]));
+  const T m0 = P::mul(m0s, P::k(kc.inv_scale));
   const T rho = P::add(P::k(1.0f), m0);
-  const T inv = P::rcp(rho);
-  const T ux = P::mul(P::add(mx, P::k(kc.hfx)), inv);
-  const T uy = P::mul(P::add(my, P::k(kc.hfy)), inv);
+  const T invs = P::mul(P::rcp(rho), P::k(kc.inv_scale));
+  const T ux = P::mul(P::add(mxs, P::k(kc.shfx)), invs);
+  const T uy = P::mul(P::add(mys, P::k(kc.shfy)), invs);
   const T usq = P::fma(ux, ux, P::mul(uy, uy));
   const T orho = P::mul(P::k(kc.omega), rho);
   const T uf = P::fma(P::k(kc.fp3fx), ux, P::mul(P::k(kc.fp3fy), uy));
   const T a = P::fma(P::k(kc.omega), m0, P::fma(P::mul(P::k(-1.5f), orho), usq, P::neg(uf)));
   const T b = P::mul(P::k(3.0f), orho), c = P::mul(P::k(4.5f), orho);
-  const T p = P::add(ux, uy), q = P::sub(uy, ux);
-  const T cu[kQ] = {P::k(0.0f), ux, uy, P::neg(ux), P::neg(uy), p, q, P::neg(p), P::neg(q)};
   const T om1 = P::k(kc.one_minus_omega);
-  out[0] = P::fma(P::k(weight<float>(0)), a, P::mul(om1, g[0]));
-#if defined(__CUDACC__)
-#pragma unroll
-#endif
-  for (int i = 1; i < kQ; ++i) {
-    const T t = P::fma(P::fma(c, cu[i], P::add(b, P::k(kc.k9[i]))), cu[i], P::add(a, P::k(kc.k3[i])));
-    out[i] = P::fma(P::k(weight<float>(i)), t, P::mul(om1, g[i]));
-  }
+  out[0] = P::fma(om1, g[0], P::mul(P::k(kc.w0), a));
+  const T wa = P::mul(P::k(kc.wax), a), wb = P::mul(P::k(kc.wax), b), wc = P::mul(P::k(kc.wax), c);
+  fast_pair<P>(g, kc, 1, 3, ux, wa, wb, wc, om1, out);
+  fast_pair<P>(g, kc, 2, 4, uy, wa, wb, wc, om1, out);
+  const T da = P::mul(P::k(kc.wdg), a), db = P::mul(P::k(kc.wdg), b), dc = P::mul(P::k(kc.wdg), c);
+  fast_pair<P>(g, kc, 5, 7, P::add(ux, uy), da, db, dc, om1, out);
+  fast_pair<P>(g, kc, 6, 8, P::sub(uy, ux), da, db, dc, om1, out);
 }
 
 LBM_HD void collide_fast(const float (&g)[kQ], const FastConsts& k, float (&out)[kQ]) {

@@ -166,6 +166,11 @@ struct PlaneScales {
   float dec[kQ];  // g = stored * dec[i]
 };
 
+// Storage scale of the 16-bit forms, the same power of two for every plane (the step kernels
+// fold it into the collision constants): |g_i| <= 2 fits FP16 (g_i = f_i - w_i of a state with
+// 0 <= f_i <= 1 lies in [-w_i, 1 - w_i]), and values down to 2^-29 stay normal.
+constexpr float kStoreScale16 = 32768.0f;
+
 __device__ __forceinline__ float to_float(__half h) { return __half2float(h); }
 __device__ __forceinline__ float to_float(__nv_bfloat16 h) { return __bfloat162float(h); }
 template <class ST>
@@ -205,7 +210,9 @@ __device__ __forceinline__ __nv_bfloat16 encode<__nv_bfloat16>(float v, int i,
   return from_float<__nv_bfloat16>(v * s.enc[i]);
 }
 
-// 16-byte vector load (read-only path) / store of kVec consecutive cells, decoded.
+// 16-byte vector load (read-only path) / store of kVec consecutive cells in the step kernels'
+// compute representation (plain forms: the values; 16-bit forms: the scaled values widened to
+// FP32, see load_vec16).
 template <class ST>
 __device__ __forceinline__ void load_vec(const ST* p, typename StoreTraits<ST>::T (&v)[StoreTraits<ST>::kVec],
                                          int plane_index, const PlaneScales& s);
@@ -225,8 +232,10 @@ __device__ __forceinline__ void load_vec<double>(const double* p, double (&v)[2]
   v[0] = t.x;
   v[1] = t.y;
 }
+// 16-bit forms: the step kernels compute on the scaled values (FastConsts carries the scale), so
+// their loads only widen to FP32.
 template <class H>
-__device__ __forceinline__ void load_vec16(const H* p, float (&v)[8], int i, const PlaneScales& s) {
+__device__ __forceinline__ void load_vec16(const H* p, float (&v)[8], int, const PlaneScales&) {
   const uint4 t = __ldg(reinterpret_cast<const uint4*>(p));
   const uint32_t w[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
@@ -235,8 +244,8 @@ __device__ __forceinline__ void load_vec16(const H* p, float (&v)[8], int i, con
     const uint16_t a = static_cast<uint16_t>(w[k] & 0xffffu), b = static_cast<uint16_t>(w[k] >> 16);
     memcpy(&lo, &a, 2);
     memcpy(&hi, &b, 2);
-    v[2 * k] = to_float(lo) * s.dec[i];
-    v[2 * k + 1] = to_float(hi) * s.dec[i];
+    v[2 * k] = to_float(lo);
+    v[2 * k + 1] = to_float(hi);
   }
 }
 template <>
@@ -288,6 +297,102 @@ __device__ __forceinline__ void store_vec<__nv_bfloat16>(__nv_bfloat16* p, const
   store_vec16(p, v, i, s);
 }
 
+// ---------------------------------------------------------------------------------------------
+// Stochastic rounding of the 16-bit storage forms.
+//
+// Round-to-nearest storage loses every per-step change smaller than half a unit in the last
+// place of the stored value: at low Mach numbers the body-force and viscous increments of g_i
+// (~1e-6) are below half an FP16 ulp of g_i (~4e-6), so the flow stagnates (measured: 10 %
+// velocity error on a developing Poiseuille channel). The step kernels therefore round the
+// encoded FP32 value v to the 16-bit format stochastically: with D the number of significand
+// bits the format drops (FP16 13, BF16 16) and r uniform in [0, 2^D), the magnitude bits of v
+// plus r are truncated (round toward zero), which rounds up with probability equal to the
+// dropped fraction, so E[stored] = v and sub-ulp increments survive on average.
+//
+// The D random bits of each value are a deterministic function of (cell pair, plane, step): a
+// 32-bit hash H of the pair's cell offset (y * pitch + x) / 2 xor the step key, rotated left by
+// 7 i bits for plane i; bits [32 - D, 32) of the rotation go to the pair's even cell and bits
+// [0, D) to its odd cell (D <= 16: disjoint fields, each uniform because H is). Fields of
+// different planes overlap, so their rounding errors are correlated, which leaves every stored
+// value unbiased. Integer rotations and masks keep this off the FP32 pipes. Every kernel variant derives them identically, so results do not depend on
+// the variant, and a run is reproducible from its step counter. The hash is the "lowbias32"
+// integer mixer (C. Wellons, hash-prospector, 2018). Values past the format's largest finite
+// value saturate (round toward zero); the finite check treats a saturated value as diverged.
+// ---------------------------------------------------------------------------------------------
+__host__ __device__ constexpr uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+__host__ __device__ constexpr int sr_plane_rot(int i) { return (7 * i) & 31; }
+// Key of lattice step t (computed on the host for each launch, or on the device from a step
+// counter in device memory for graph-captured launches).
+__host__ __device__ constexpr uint32_t sr_step_key(uint32_t t) { return mix32(t * 0x9e3779b9u + 0x7f4a7c15u); }
+// Hash of the cell pair whose even cell sits at cell offset `cell` (y * pitch + x + base).
+__device__ __forceinline__ uint32_t sr_pair_hash(long long cell, uint32_t rkey) {
+  return mix32(static_cast<uint32_t>(cell >> 1) ^ rkey);
+}
+
+template <class ST>
+struct SrFormat;
+template <>
+struct SrFormat<__half> {
+  static constexpr int kDrop = 13;
+};
+template <>
+struct SrFormat<__nv_bfloat16> {
+  static constexpr int kDrop = 16;
+};
+
+template <class ST>
+__device__ __forceinline__ uint32_t cvt_rz_pair(float lo, float hi);
+template <>
+__device__ __forceinline__ uint32_t cvt_rz_pair<__half>(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+template <>
+__device__ __forceinline__ uint32_t cvt_rz_pair<__nv_bfloat16>(float lo, float hi) {
+  uint32_t d;
+  asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
+  return d;
+}
+
+// Stochastically rounded pair of plane-i values, already scaled (lo = even cell, in the low
+// half).
+template <class ST>
+__device__ __forceinline__ uint32_t encode_pair_sr(float lo, float hi, int i, uint32_t pair_hash) {
+  constexpr int D = SrFormat<ST>::kDrop;
+  const uint32_t h = __funnelshift_l(pair_hash, pair_hash, sr_plane_rot(i));
+  const uint32_t r0 = h >> (32 - D);
+  const uint32_t r1 = h & ((1u << D) - 1u);
+  const float a = __uint_as_float(__float_as_uint(lo) + r0);
+  const float b = __uint_as_float(__float_as_uint(hi) + r1);
+  return cvt_rz_pair<ST>(a, b);
+}
+
+// True for a stored 16-bit value at the format's largest finite magnitude (saturated).
+template <class ST>
+__device__ __forceinline__ bool stored_saturated(ST) {
+  return false;
+}
+template <>
+__device__ __forceinline__ bool stored_saturated<__half>(__half v) {
+  uint16_t b;
+  memcpy(&b, &v, 2);
+  return (b & 0x7fffu) == 0x7bffu;
+}
+template <>
+__device__ __forceinline__ bool stored_saturated<__nv_bfloat16>(__nv_bfloat16 v) {
+  uint16_t b;
+  memcpy(&b, &v, 2);
+  return (b & 0x7fffu) == 0x7f7fu;
+}
+
 // G consecutive cells as one aligned vector of G * sizeof(ST) bytes (8 or 16), decoded /
 // encoded; generalises load_vec / store_vec to the narrower vectors of the cells-per-thread
 // tuning dimension.
@@ -317,7 +422,7 @@ struct VecIO<float, 2> {
 };
 template <class H>
 struct VecIO16x4 {
-  static __device__ __forceinline__ void load(const H* p, float (&v)[4], int i, const PlaneScales& s) {
+  static __device__ __forceinline__ void load(const H* p, float (&v)[4], int, const PlaneScales&) {
     const uint2 t = __ldg(reinterpret_cast<const uint2*>(p));
     const uint32_t w[2] = {t.x, t.y};
 #pragma unroll
@@ -326,8 +431,8 @@ struct VecIO16x4 {
       const uint16_t a = static_cast<uint16_t>(w[k] & 0xffffu), b = static_cast<uint16_t>(w[k] >> 16);
       memcpy(&lo, &a, 2);
       memcpy(&hi, &b, 2);
-      v[2 * k] = to_float(lo) * s.dec[i];
-      v[2 * k + 1] = to_float(hi) * s.dec[i];
+      v[2 * k] = to_float(lo);
+      v[2 * k + 1] = to_float(hi);
     }
   }
   static __device__ __forceinline__ void store(H* p, const float (&v)[4], int i, const PlaneScales& s) {
@@ -354,6 +459,18 @@ __device__ __forceinline__ typename StoreTraits<ST>::T load_one(const ST* p, int
                                                                 const PlaneScales& s) {
   return decode<ST>(__ldg(p), i, s);
 }
+// One value in the step kernels' compute representation (16-bit forms: scaled, widened).
+template <class ST>
+__device__ __forceinline__ typename StoreTraits<ST>::T widen(ST v) {
+  if constexpr (sizeof(ST) == 2)
+    return to_float(v);
+  else
+    return v;
+}
+template <class ST>
+__device__ __forceinline__ typename StoreTraits<ST>::T load_step(const ST* p) {
+  return widen<ST>(__ldg(p));
+}
 
 // ---------------------------------------------------------------------------------------------
 // Bit-packed mask
@@ -372,6 +489,35 @@ __device__ __forceinline__ bool mask_solid(const uint32_t* __restrict__ mask, in
 // ---------------------------------------------------------------------------------------------
 // Geometry of one instance on the device
 // ---------------------------------------------------------------------------------------------
+// Step-kernel store of G consecutive cells x0 .. x0 + G - 1 of plane i (x0 even): plain forms
+// store the values, 16-bit forms round each pair k of scaled values stochastically with pair
+// hash ph[k].
+template <class ST, int G>
+struct StepStore {
+  static constexpr bool kSr = sizeof(ST) == 2;
+  static constexpr int kPairs = kSr ? G / 2 : 1;
+  static __device__ __forceinline__ void hashes(long long cell0, uint32_t rkey, uint32_t (&ph)[kPairs]) {
+#pragma unroll
+    for (int k = 0; k < kPairs; ++k) ph[k] = kSr ? sr_pair_hash(cell0 + 2 * k, rkey) : 0u;
+  }
+  static __device__ __forceinline__ void store(ST* p, const typename StoreTraits<ST>::T (&v)[G], int i,
+                                               const PlaneScales& s, const uint32_t (&ph)[kPairs]) {
+    if constexpr (kSr) {
+      static_assert(G == 4 || G == 8, "16-bit stores are 8 or 16 bytes");
+      uint32_t w[G / 2];
+#pragma unroll
+      for (int k = 0; k < G / 2; ++k) w[k] = encode_pair_sr<ST>(v[2 * k], v[2 * k + 1], i, ph[k]);
+      if constexpr (G == 8)
+        *reinterpret_cast<uint4*>(p) = make_uint4(w[0], w[1], w[2], w[3]);
+      else
+        *reinterpret_cast<uint2*>(p) = make_uint2(w[0], w[1]);
+    } else {
+      (void)ph;
+      VecIO<ST, G>::store(p, v, i, s);
+    }
+  }
+};
+
 struct Grid2D {
   int nx, ny, pitch;
   int mask_words;

@@ -53,7 +53,7 @@ struct Form<__half> {
   using Phys = FastPhys;
   using PackedPhys = Phys;  // already packed
   static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_fast_consts(float(tau), float(fx), float(fy));
+    return make_fast_consts(float(tau), float(fx), float(fy), kStoreScale16);
   }
 };
 template <>
@@ -62,7 +62,7 @@ struct Form<__nv_bfloat16> {
   using Phys = FastPhys;
   using PackedPhys = Phys;  // already packed
   static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_fast_consts(float(tau), float(fx), float(fy));
+    return make_fast_consts(float(tau), float(fx), float(fy), kStoreScale16);
   }
 };
 
@@ -112,6 +112,15 @@ Eq9<typename StoreTraits<ST>::T> inlet_eq(const lbm_solver* s) {
   return host_equilibrium<T>(T(1), T(s->u_in), T(0));
 }
 
+// The inlet equilibrium in the step kernels' compute representation (16-bit forms: scaled).
+template <class ST>
+Eq9<typename StoreTraits<ST>::T> step_inlet_eq(const lbm_solver* s) {
+  Eq9<typename StoreTraits<ST>::T> e = inlet_eq<ST>(s);
+  if (sizeof(ST) == 2)
+    for (int i = 0; i < kQ; ++i) e.v[i] *= s->sc.enc[i];
+  return e;
+}
+
 // Physics of a launch: the scalar form, or (kPacked) its two-cells-per-instruction twin.
 template <class ST, bool kPacked>
 using PhysOf = std::conditional_t<kPacked, typename Form<ST>::PackedPhys, typename Form<ST>::Phys>;
@@ -127,7 +136,7 @@ int launch_steps_t(lbm_solver* s, int steps) {
   a.cpr = (s->nx + 32 * G - 1) / (32 * G);
   a.items = s->ny * a.cpr;
   a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
-  const Eq9<T> e = inlet_eq<ST>(s);
+  const Eq9<T> e = step_inlet_eq<ST>(s);
   for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
   a.sc = s->sc;
   const auto kernel = pull_step_kernel<ST, Phys, kOpen, kVariant>;
@@ -143,6 +152,7 @@ int launch_steps_t(lbm_solver* s, int steps) {
   for (int k = 0; k < steps; ++k) {
     a.src = static_cast<const ST*>(s->buf[s->cur]);
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+    a.rkey = sr_step_key(s->t++);
     kernel<<<grid, s->block, 0, s->stream>>>(a);
     s->cur ^= 1;
   }
@@ -162,7 +172,7 @@ int launch_tma_t(lbm_solver* s, int steps) {
   a.cpr = (s->nx + 32 * S::G - 1) / (32 * S::G);
   a.items = s->ny * a.cpr;
   a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
-  const Eq9<T> e = inlet_eq<ST>(s);
+  const Eq9<T> e = step_inlet_eq<ST>(s);
   for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
   a.sc = s->sc;
   const int tpr = (s->nx + S::TW - 1) / S::TW;
@@ -181,6 +191,7 @@ int launch_tma_t(lbm_solver* s, int steps) {
   for (int k = 0; k < steps; ++k) {
     a.src = static_cast<const ST*>(s->buf[s->cur]);
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+    a.rkey = sr_step_key(s->t++);
     kernel<<<grid, kTmaThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
     s->cur ^= 1;
   }
@@ -201,7 +212,7 @@ int launch_async_t(lbm_solver* s, int steps) {
   a.cpr = (s->nx + 32 * G - 1) / (32 * G);
   a.items = s->ny * a.cpr;
   a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
-  const Eq9<T> e = inlet_eq<ST>(s);
+  const Eq9<T> e = step_inlet_eq<ST>(s);
   for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
   a.sc = s->sc;
   const auto kernel = pull_step_async_kernel<ST, Phys, kOpen, kDepth>;
@@ -219,6 +230,7 @@ int launch_async_t(lbm_solver* s, int steps) {
   for (int k = 0; k < steps; ++k) {
     a.src = static_cast<const ST*>(s->buf[s->cur]);
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+    a.rkey = sr_step_key(s->t++);
     kernel<<<grid, kBlock, smem, s->stream>>>(a);
     s->cur ^= 1;
   }
@@ -226,27 +238,24 @@ int launch_async_t(lbm_solver* s, int steps) {
   return LBM_OK;
 }
 
-// Warp-specialised ring with one cell per lane (step_ring.cuh); plain FP32 / FP64 storage only
-// (the 16-bit forms run the bulk-copy kernel of variant 4 instead).
+// Warp-specialised ring with one cell (plain FP32 / FP64) or one pair of cells (16-bit storage)
+// per lane (step_ring.cuh).
 template <class ST, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 int launch_ring_t(lbm_solver* s, int steps) {
-  if constexpr (!std::is_same<ST, float>::value && !std::is_same<ST, double>::value) {
-    return launch_tma_t<ST, kOpen, 2>(s, steps);
-  } else {
-    using A = typename Form<ST>::A;
-    using Phys = ExactPhys<A>;
+  {
+    using Phys = typename Form<ST>::Phys;
     using T = typename StoreTraits<ST>::T;
     using S = RingShape<ST, kW, kC>;
     StepArgs<ST, Phys> a{};
     a.mask = s->mask_d;
     a.g = s->g;
     a.k = Form<ST>::consts(s->tau, s->fx, s->fy);
-    const Eq9<T> e = inlet_eq<ST>(s);
+    const Eq9<T> e = step_inlet_eq<ST>(s);
     for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
     a.sc = s->sc;
     const int tpr = (s->nx + S::TW - 1) / S::TW;
     const int tiles = tpr * s->ny;
-    const auto kernel = pull_step_ring_kernel<ST, A, kOpen, kW, kC, kStages, kMinBlocks>;
+    const auto kernel = pull_step_ring_kernel<ST, Phys, kOpen, kW, kC, kStages, kMinBlocks>;
     const size_t smem = ring_smem_bytes<S>(kStages);
     LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem)));
@@ -260,6 +269,7 @@ int launch_ring_t(lbm_solver* s, int steps) {
     for (int k = 0; k < steps; ++k) {
       a.src = static_cast<const ST*>(s->buf[s->cur]);
       a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
+      a.rkey = sr_step_key(s->t++);
       kernel<<<grid, S::kThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
       s->cur ^= 1;
     }
@@ -270,21 +280,16 @@ int launch_ring_t(lbm_solver* s, int steps) {
 
 constexpr int kMaskPadWords = 80;
 
-// Automatic kernel choice (variant < 0). Plain FP32 / FP64: the one-cell-per-lane ring (12) when
-// there are at least two tiles per SM, the direct kernel (0) otherwise. 16-bit forms: the
-// bulk-copy kernel (4) when the rows hold whole tiles and there are enough tiles to fill the GPU,
-// the direct kernel otherwise (narrow or small grids, where most consumer warps would idle).
+// Automatic kernel choice (variant < 0): the ring kernel when there are at least two of its
+// tiles per SM (plain FP32 / FP64: 12, 63 registers, 3 resident blocks; 16-bit storage: 17, the
+// same shape capped at 72 registers for 3 resident blocks), the direct kernel (0) otherwise
+// (small grids, where most consumer warps would idle).
 template <class ST>
 int auto_variant(const lbm_solver* s) {
-  if constexpr (std::is_same<ST, float>::value || std::is_same<ST, double>::value) {
-    using S = RingShape<ST, 8, 2>;
-    const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
-    return tiles >= 2LL * s->sm_count ? 12 : 0;
-  } else {
-    using S = TmaShape<ST>;
-    const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
-    return (s->nx >= S::TW && tiles >= 4LL * s->sm_count) ? 4 : 0;
-  }
+  using S = RingShape<ST, 8, 2>;
+  const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
+  if (tiles < 2LL * s->sm_count) return 0;
+  return sizeof(ST) == 2 ? 17 : 12;
 }
 
 template <class ST, bool kOpen>
@@ -307,6 +312,7 @@ int launch_steps_o(lbm_solver* s, int steps) {
     case 14: return launch_ring_t<ST, kOpen, 8, 2, 2, 4>(s, steps);
     case 15: return launch_ring_t<ST, kOpen, 4, 2, 3, 1>(s, steps);
     case 16: return launch_ring_t<ST, kOpen, 4, 2, 3, 7>(s, steps);
+    case 17: return launch_ring_t<ST, kOpen, 8, 2, 2, 3>(s, steps);
     default: return launch_steps_t<ST, kOpen, 0>(s, steps);
   }
 }
@@ -420,12 +426,10 @@ int check(const lbm_solver* s) { return s ? LBM_OK : LBM_ERR_INVALID_ARG; }
 // smallest values of interest (~1e-9) still above the FP16 subnormal range.
 PlaneScales default_scales(int precision) {
   PlaneScales p{};
+  const bool s16 = precision == LBM_FP16_STORE || precision == LBM_BF16_STORE;
   for (int i = 0; i < kQ; ++i) {
-    const int e = precision == LBM_FP16_STORE || precision == LBM_BF16_STORE
-                      ? (i == 0 ? 15 : (i <= 4 ? 17 : 18))
-                      : 0;
-    p.enc[i] = std::ldexp(1.0f, e);
-    p.dec[i] = std::ldexp(1.0f, -e);
+    p.enc[i] = s16 ? kStoreScale16 : 1.0f;
+    p.dec[i] = s16 ? 1.0f / kStoreScale16 : 1.0f;
   }
   return p;
 }
@@ -791,8 +795,8 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
 
 int lbm_set_variant(lbm_solver* s, int variant) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
-  if (variant < -1 || variant > 16)
-    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 16]");
+  if (variant < -1 || variant > 17)
+    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 17]");
   s->variant = variant;
   return LBM_OK;
 }

@@ -17,6 +17,7 @@ struct lbm_solver {
   int host_elem = 4;  // bytes per host value (float, or double for FP64)
   void* buf[2] = {nullptr, nullptr};  // pull states; buf[cur] is the current one
   int cur = 0;
+  uint32_t t = 0;  // lattice steps taken (stochastic-rounding key of the 16-bit forms)
   size_t state_bytes = 0;
   uint32_t* mask_d = nullptr;  // bit-packed mask with periodic ghost bits
   std::vector<uint8_t> solid;  // host copy (the reference's solid())

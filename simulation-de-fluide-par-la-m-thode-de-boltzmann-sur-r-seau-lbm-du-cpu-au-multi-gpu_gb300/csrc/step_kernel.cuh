@@ -35,11 +35,14 @@ struct StepArgs {
   typename Phys::Consts k;
   T eq_in[kQ];  // inlet equilibrium (open domain)
   PlaneScales sc;
+  uint32_t rkey;       // stochastic-rounding key of this step (16-bit forms)
+  long long key_base;  // cell offset of this grid in the rounding hash (batched instances)
 };
 
 // Exact (bit-for-bit with v0) physics, one cell at a time (FP64).
 template <class A>
 struct ExactPhys {
+  using Arith = A;
   using T = typename A::T;
   using Consts = CollideConsts<T>;
   template <int G>
@@ -184,7 +187,7 @@ __device__ __forceinline__ void process_chunk(const StepArgs<ST, Phys>& p, const
       // cell x0 + k reads x0 + k - 1: shift up, the first element from the lane to the left
       T left = __shfl_up_sync(0xffffffffu, v[i][G - 1], 1);
       if (lane == 0) {  // lane 0 is always active (a chunk exists only if it holds cells)
-        if (!kOpen || x0 > 0) left = load_one<ST>(rowp + (x0 > 0 ? x0 - 1 : nx - 1), i, p.sc);
+        if (!kOpen || x0 > 0) left = load_step<ST>(rowp + (x0 > 0 ? x0 - 1 : nx - 1));
       }
 #pragma unroll
       for (int k = G - 1; k > 0; --k) v[i][k] = v[i][k - 1];
@@ -192,7 +195,7 @@ __device__ __forceinline__ void process_chunk(const StepArgs<ST, Phys>& p, const
     } else if (dir_cx(i) == -1) {
       // cell x0 + k reads x0 + k + 1: shift down, the last element from the lane to the right
       T right = __shfl_down_sync(0xffffffffu, v[i][0], 1);
-      if (lane == 31 && c.active) right = load_one<ST>(rowp + (x0 + G < nx ? x0 + G : 0), i, p.sc);
+      if (lane == 31 && c.active) right = load_step<ST>(rowp + (x0 + G < nx ? x0 + G : 0));
 #pragma unroll
       for (int k = 0; k < G - 1; ++k) v[i][k] = v[i][k + 1];
       v[i][G - 1] = right;
@@ -200,7 +203,7 @@ __device__ __forceinline__ void process_chunk(const StepArgs<ST, Phys>& p, const
         // periodic wrap: cell nx - 1 reads x = 0
         const int kl = nx - 1 - x0;
         if (kl >= 0 && kl < G) {
-          const T w = load_one<ST>(rowp, i, p.sc);
+          const T w = load_step<ST>(rowp);
 #pragma unroll
           for (int k = 0; k < G; ++k)
             if (k == kl) v[i][k] = w;
@@ -247,12 +250,10 @@ __device__ __forceinline__ void process_chunk(const StepArgs<ST, Phys>& p, const
         const uint32_t w = dir_cy(i) == 1 ? wm : (dir_cy(i) == -1 ? wp : w0);
         const bool solid_src = (w >> (kl + 1)) & 1u;
         const T val = solid_src
-                          ? load_one<ST>(p.src + dir_opp(i) * plane +
-                                             static_cast<long long>(y) * pitch + (nx - 2),
-                                         dir_opp(i), p.sc)
-                          : load_one<ST>(p.src + i * plane + static_cast<long long>(r) * pitch +
-                                             (nx - 1),
-                                         i, p.sc);
+                          ? load_step<ST>(p.src + dir_opp(i) * plane +
+                                             static_cast<long long>(y) * pitch + (nx - 2))
+                          : load_step<ST>(p.src + i * plane + static_cast<long long>(r) * pitch +
+                                             (nx - 1));
 #pragma unroll
         for (int k = 0; k < G; ++k)
           if (k == kl) v[i][k] = val;
@@ -267,9 +268,12 @@ __device__ __forceinline__ void process_chunk(const StepArgs<ST, Phys>& p, const
   T out[kQ][G];
   Phys::template collide_all<G>(v, p.k, out);
   if (c.active) {
+    using SS = StepStore<ST, G>;
+    uint32_t ph[SS::kPairs];
+    SS::hashes(p.key_base + static_cast<long long>(y) * pitch + x0, p.rkey, ph);
 #pragma unroll
     for (int i = 0; i < kQ; ++i)
-      VecIO<ST, G>::store(p.dst + i * plane + static_cast<long long>(y) * pitch + x0, out[i], i, p.sc);
+      SS::store(p.dst + i * plane + static_cast<long long>(y) * pitch + x0, out[i], i, p.sc, ph);
   }
 }
 

@@ -1,4 +1,5 @@
-// Warp-specialised pull stream-collide step, one cell per lane (plain FP32 / FP64 storage).
+// Warp-specialised pull stream-collide step, one cell (plain FP32 / FP64 storage) or one pair of
+// cells (16-bit storage) per lane.
 // Same results as pull_step_kernel (step_kernel.cuh); same producer as pull_step_tma_kernel
 // (step_tma.cuh), different consumers:
 //
@@ -7,10 +8,12 @@
 //     and, on a periodic row's first and last tile, the 16-byte blocks holding the wrapped
 //     neighbours (cell nx - 1 of the 3 planes moving right, cell 0 of the 3 moving left) into a
 //     shared ring stage with cp.async.bulk, completing on the stage's "full" mbarrier;
-//   * consumer warp w owns the strip of 32 * kC cells tx0 + w * 32 kC .., and lane l the cells
-//     strip + 32 c + l (c = 0 .. kC - 1): consecutive lanes hold consecutive cells, so each
-//     plane value is one conflict-free shared load at offset -c_x, and each of the 9 results is
-//     one fully coalesced 32 * element-size warp store;
+//   * consumer warp w owns a strip of 32 * kC * LC cells (LC = 1, or 2 for 16-bit storage), and
+//     lane l the cells strip + 32 LC c + LC l .. + LC - 1 (c = 0 .. kC - 1): consecutive lanes
+//     hold consecutive cells, so each plane value is one conflict-free 4- or 8-byte shared load
+//     at offset -c_x (16-bit pairs: two aligned 4-byte loads and a byte permute for the shifted
+//     planes), and each of the 9 results is one fully coalesced warp store of 128 bytes (FP64:
+//     256 bytes);
 //   * a lane keeps one cell live at a time (9 inputs, 9 outputs, the collision's temporaries),
 //     which leaves registers for many resident warps: the exact collision is a long chain of
 //     dependent IEEE operations, and warps are what hides its latency;
@@ -27,7 +30,9 @@ namespace lbm_b200 {
 template <class ST, int kW, int kC>
 struct RingShape {
   static constexpr int H = 16 / static_cast<int>(sizeof(ST));  // halo elements (16 bytes)
-  static constexpr int SW = 32 * kC;                            // strip width (cells per warp)
+  static constexpr int LC = sizeof(ST) == 2 ? 2 : 1;            // cells per lane per pass
+  static constexpr int SW = 32 * kC * LC;                       // strip width (cells per warp)
+  static constexpr int WPS = SW / 32;                            // mask words per strip
   static constexpr int TW = kW * SW;                            // tile width
   static constexpr int SROW = TW + 2 * H;
   static constexpr int MW = TW / 32 + 4;  // staged mask words per row
@@ -118,9 +123,112 @@ __device__ __forceinline__ void ring_cell(const StepArgs<ST, ExactPhys<A>>& p, c
   for (int i = 0; i < kQ; ++i) d[i * plane] = out[i];
 }
 
-template <class ST, class A, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
+// 16-bit storage: widen a packed pair of stored (scaled) values to FP32, element 0 in the low
+// half (the compute representation of the step kernels).
+template <class ST>
+__device__ __forceinline__ float2 widen_pair(uint32_t raw);
+template <>
+__device__ __forceinline__ float2 widen_pair<__half>(uint32_t raw) {
+  __half2 h;
+  memcpy(&h, &raw, 4);
+  return __half22float2(h);
+}
+template <>
+__device__ __forceinline__ float2 widen_pair<__nv_bfloat16>(uint32_t raw) {
+  __nv_bfloat162 h;
+  memcpy(&h, &raw, 4);
+  return __bfloat1622float2(h);
+}
+
+// One pair of cells x, x + 1 (x even) of a strip, 16-bit storage, FP32 fast collision. Same
+// stage layout as ring_cell; word / lane locate the pair's mask bits (cells x - 1 .. x + 2).
+template <class ST, bool kOpen, class S>
+__device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const ST* st,
+                                          const uint32_t* sm, const ST* wr, int y, int x, int lx,
+                                          int word, int lane, bool solids) {
+  const int nx = p.g.nx;
+  const long long plane = p.g.plane;
+  const long long row = static_cast<long long>(y) * p.g.pitch;
+  float2 v[kQ];
+#pragma unroll
+  for (int i = 0; i < kQ; ++i) {
+    const uint32_t* r = reinterpret_cast<const uint32_t*>(st + i * S::SROW + lx);
+    const uint32_t own = r[0];
+    uint32_t raw = own;
+    if (dir_cx(i) == 1) raw = __byte_perm(r[-1], own, 0x5432);   // cells x - 1, x
+    if (dir_cx(i) == -1) raw = __byte_perm(own, r[1], 0x5432);   // cells x + 1, x + 2
+    v[i] = widen_pair<ST>(raw);
+  }
+  if (!kOpen) {
+    if (x == 0) {
+      const int k = (nx - 1) & (S::H - 1);
+      v[1].x = widen<ST>(wr[0 * S::H + k]);
+      v[5].x = widen<ST>(wr[1 * S::H + k]);
+      v[8].x = widen<ST>(wr[2 * S::H + k]);
+    }
+    if (x == nx - 1) {
+      v[3].x = widen<ST>(wr[3 * S::H]);
+      v[6].x = widen<ST>(wr[4 * S::H]);
+      v[7].x = widen<ST>(wr[5 * S::H]);
+    }
+    if (x + 1 == nx - 1) {
+      v[3].y = widen<ST>(wr[3 * S::H]);
+      v[6].y = widen<ST>(wr[4 * S::H]);
+      v[7].y = widen<ST>(wr[5 * S::H]);
+    }
+  }
+  uint32_t nm = 0, n0 = 0, np = 0;  // bits 0..3: cells x - 1 .. x + 2 of rows y - 1, y, y + 1
+  if (solids) {
+    const int q = word + (lane >> 4), sh = (2 * lane) & 31;
+    nm = __funnelshift_r(sm[q], sm[q + 1], sh) & 15u;
+    n0 = __funnelshift_r(sm[S::MW + q], sm[S::MW + q + 1], sh) & 15u;
+    np = __funnelshift_r(sm[2 * S::MW + q], sm[2 * S::MW + q + 1], sh) & 15u;
+    if ((nm | n0 | np) != 0u) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        if ((n0 >> (1 + k)) & 1u) continue;  // solid cell: its slots are never read
+#pragma unroll
+        for (int i = 1; i < kQ; ++i) {
+          const uint32_t w = dir_cy(i) == 1 ? nm : (dir_cy(i) == -1 ? np : n0);
+          if ((w >> (1 + k - dir_cx(i))) & 1u) {
+            const float b = load_step<ST>(p.src + dir_opp(i) * plane + row + x + k);
+            if (k == 0) v[i].x = b; else v[i].y = b;
+          }
+        }
+      }
+    }
+  }
+  if (kOpen) {
+    if (x == 0) {
+      v[1].x = p.eq_in[1];
+      v[5].x = p.eq_in[5];
+      v[8].x = p.eq_in[8];
+    }
+#pragma unroll
+    for (int k = 0; k < 2; ++k) {
+      if (x + k != nx - 1) continue;
+#pragma unroll
+      for (int i = 1; i < kQ; ++i) {
+        if (dir_cx(i) != -1) continue;
+        const uint32_t w = dir_cy(i) == 1 ? nm : (dir_cy(i) == -1 ? np : n0);
+        const float val = ((w >> (1 + k)) & 1u)
+                              ? load_step<ST>(p.src + dir_opp(i) * plane + row + (nx - 2))
+                              : widen<ST>(st[i * S::SROW + lx + k]);
+        if (k == 0) v[i].x = val; else v[i].y = val;
+      }
+    }
+  }
+  float2 out[kQ];
+  collide_fast_t<FastF32x2>(v, p.k, out);
+  const uint32_t ph = sr_pair_hash(p.key_base + row + x, p.rkey);
+  uint32_t* d = reinterpret_cast<uint32_t*>(p.dst + row + x);
+#pragma unroll
+  for (int i = 0; i < kQ; ++i) d[i * (plane / 2)] = encode_pair_sr<ST>(out[i].x, out[i].y, i, ph);
+}
+
+template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
-    pull_step_ring_kernel(const StepArgs<ST, ExactPhys<A>> p, int tiles_per_row, int tiles, int* err) {
+    pull_step_ring_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
   using S = RingShape<ST, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);
@@ -220,16 +328,21 @@ __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
       const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes);
       const int ym = y == 0 ? ny - 1 : y - 1;
       const int yp = y == ny - 1 ? 0 : y + 1;
-      const int w0 = cw * kC;  // first staged mask word of the strip
-      // Any solid among the strip's cells and their neighbours (words w0 .. w0 + kC of 3 rows).
+      const int w0 = cw * S::WPS;  // first staged mask word of the strip
+      // Any solid among the strip's cells and their neighbours (words w0 .. w0 + WPS of 3 rows).
       uint32_t mine = 0;
-      if (lane < 3 * (kC + 1)) mine = sm[(lane / (kC + 1)) * S::MW + w0 + lane % (kC + 1)];
+      if (lane < 3 * (S::WPS + 1)) mine = sm[(lane / (S::WPS + 1)) * S::MW + w0 + lane % (S::WPS + 1)];
       const bool solids = __any_sync(0xffffffffu, mine != 0u);
 #pragma unroll 1
       for (int c = 0; c < kC; ++c) {
-        const int x = xw + 32 * c + lane;
-        if (x < nx)
-          ring_cell<ST, A, kOpen, S>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H, w0 + c, lane, solids);
+        const int x = xw + 32 * S::LC * c + S::LC * lane;
+        if (x < nx) {
+          if constexpr (S::LC == 2)
+            ring_pair<ST, kOpen, S>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids);
+          else
+            ring_cell<ST, typename Phys::Arith, kOpen, S>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H,
+                                                         w0 + c, lane, solids);
+        }
       }
     }
     __syncwarp();

@@ -123,7 +123,7 @@ __device__ __forceinline__ void lds_vec<double>(const double* p, double (&v)[2],
   v[1] = t.y;
 }
 template <class H>
-__device__ __forceinline__ void lds_vec16(const H* p, float (&v)[8], int i, const PlaneScales& s) {
+__device__ __forceinline__ void lds_vec16(const H* p, float (&v)[8], int, const PlaneScales&) {
   const uint4 t = *reinterpret_cast<const uint4*>(p);
   const uint32_t w[4] = {t.x, t.y, t.z, t.w};
 #pragma unroll
@@ -132,8 +132,8 @@ __device__ __forceinline__ void lds_vec16(const H* p, float (&v)[8], int i, cons
     const uint16_t a = static_cast<uint16_t>(w[k] & 0xffffu), b = static_cast<uint16_t>(w[k] >> 16);
     memcpy(&lo, &a, 2);
     memcpy(&hi, &b, 2);
-    v[2 * k] = to_float(lo) * s.dec[i];
-    v[2 * k + 1] = to_float(hi) * s.dec[i];
+    v[2 * k] = to_float(lo);  // scaled values (compute representation of the step kernels)
+    v[2 * k + 1] = to_float(hi);
   }
 }
 template <>
@@ -147,8 +147,8 @@ __device__ __forceinline__ void lds_vec<__nv_bfloat16>(const __nv_bfloat16* p, f
 }
 
 template <class ST>
-__device__ __forceinline__ typename StoreTraits<ST>::T lds_one(const ST* p, int i, const PlaneScales& s) {
-  return decode<ST>(*p, i, s);
+__device__ __forceinline__ typename StoreTraits<ST>::T lds_one(const ST* p, int, const PlaneScales&) {
+  return widen<ST>(*p);
 }
 
 // Mask window of cells x0 - 1 .. x0 + 30 from a staged mask row whose word 0 is word wb of the
@@ -196,7 +196,7 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
         left = lds_one<ST>(row + lx - 1, i, p.sc);
       } else {
         const ST* g = p.src + i * plane + static_cast<long long>(src_row(i, y, ym, yp)) * pitch;
-        left = kOpen ? T(0) : load_one<ST>(g + (nx - 1), i, p.sc);
+        left = kOpen ? T(0) : load_step<ST>(g + (nx - 1));
       }
 #pragma unroll
       for (int k = G - 1; k > 0; --k) v[i][k] = v[i][k - 1];
@@ -211,7 +211,7 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
         const int kl = nx - 1 - x0;  // periodic wrap: cell nx - 1 reads x = 0
         if (kl >= 0 && kl < G) {
           const ST* g = p.src + i * plane + static_cast<long long>(src_row(i, y, ym, yp)) * pitch;
-          const T w = load_one<ST>(g, i, p.sc);
+          const T w = load_step<ST>(g);
 #pragma unroll
           for (int k = 0; k < G; ++k)
             if (k == kl) v[i][k] = w;
@@ -229,7 +229,7 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
       if (bounce) {
         T b[G];
         load_vec<ST>(p.src + dir_opp(i) * plane + static_cast<long long>(y) * pitch + x0, b,
-                     dir_opp(i), p.sc);
+                     dir_opp(i), p.sc);  // step representation
 #pragma unroll
         for (int k = 0; k < G; ++k)
           if ((bounce >> k) & 1u) v[i][k] = b[k];
@@ -252,9 +252,8 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
         const uint32_t w = dir_cy(i) == 1 ? wm : (dir_cy(i) == -1 ? wp : w0);
         const bool solid_src = (w >> (kl + 1)) & 1u;
         const T val = solid_src
-                          ? load_one<ST>(p.src + dir_opp(i) * plane + static_cast<long long>(y) * pitch + (nx - 2),
-                                         dir_opp(i), p.sc)
-                          : load_one<ST>(p.src + i * plane + static_cast<long long>(r) * pitch + (nx - 1), i, p.sc);
+                          ? load_step<ST>(p.src + dir_opp(i) * plane + static_cast<long long>(y) * pitch + (nx - 2))
+                          : load_step<ST>(p.src + i * plane + static_cast<long long>(r) * pitch + (nx - 1));
 #pragma unroll
         for (int k = 0; k < G; ++k)
           if (k == kl) v[i][k] = val;
@@ -264,9 +263,12 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
 
   T out[kQ][G];
   Phys::template collide_all<G>(v, p.k, out);
+  using SS = StepStore<ST, G>;
+  uint32_t ph[SS::kPairs];
+  SS::hashes(p.key_base + static_cast<long long>(y) * pitch + x0, p.rkey, ph);
 #pragma unroll
   for (int i = 0; i < kQ; ++i)
-    store_vec<ST>(p.dst + i * plane + static_cast<long long>(y) * pitch + x0, out[i], i, p.sc);
+    SS::store(p.dst + i * plane + static_cast<long long>(y) * pitch + x0, out[i], i, p.sc, ph);
 }
 
 template <class ST, class Phys, bool kOpen, int kStages>

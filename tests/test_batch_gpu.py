@@ -77,3 +77,30 @@ def test_fp16_batch_close_to_fp32(gpu_lib, orc, specs):
             assert np.linalg.norm(x - y) / np.linalg.norm(x) < 5e-3
         for k in range(len(sub)):
             assert abs(h.total_mass(k) - a.total_mass(k)) / a.total_mass(k) < 1e-5
+
+
+def test_fp16_batched_equals_separate_launches(gpu_lib, orc, specs):
+    """The 16-bit forms round stochastically with keys from the step counter: graph replays,
+    direct launches and per-instance launches give the same bits."""
+    sub = specs[:8]
+    with gpu_lib.Batch(sub, precision="fp16") as a, gpu_lib.Batch(sub, precision="fp16") as b:
+        _fill(a, sub, orc)
+        _fill(b, sub, orc)
+        a.run(130)
+        b.run_separate(130)
+        for k in range(len(sub)):
+            assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k}"
+
+
+def test_fp16_autotune_keeps_trajectory(gpu_lib, orc, specs, tmp_path):
+    """Autotuning restores the state and the step counter: the run continues as if untouched."""
+    sub = specs[:8]
+    with gpu_lib.Batch(sub, precision="fp16") as a, gpu_lib.Batch(sub, precision="fp16") as b:
+        _fill(a, sub, orc)
+        _fill(b, sub, orc)
+        a.run(10)
+        a.autotune(tmp_path / "tune16.txt")
+        a.run(70)
+        b.run(80)
+        for k in range(len(sub)):
+            assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k}"

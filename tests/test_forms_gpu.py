@@ -1,0 +1,88 @@
+"""16-bit storage forms (FP16 / BF16 populations f_i - w_i with per-plane power-of-two scales,
+FP32 collision, FP64 mass reduction) on the GPU.
+
+* Every step-kernel variant gives the same bits for a 16-bit form (the per-cell arithmetic does
+  not depend on how cells are grouped).
+* Accuracy against the FP64 form (bit-exact with the reference's double v0): relative velocity
+  L2 error over fluid cells and mass drift, on a developing Poiseuille channel and on the
+  cylinder-wake geometry. FP16 must stay within 1e-3 (velocity); BF16 (8 significand bits) is
+  reported against a looser bound.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import golden_cases, initial_state, load_golden
+
+pytestmark = pytest.mark.gpu
+
+FORMS = ["fp16", "bf16"]
+VARIANTS = list(range(18))
+VELOCITY_L2_MAX = {"fp16": 1e-3, "bf16": 1e-2}
+
+
+@pytest.mark.parametrize("form", FORMS)
+@pytest.mark.parametrize("name", ["c1_block", "cylinder_open", "periodic_scatter", "odd_width_disc",
+                                  "tiny_1x5", "tiny_2x4", "open_seeded"])
+def test_16bit_form_identical_across_variants(gpu_lib, name, form):
+    case = golden_cases()[name]
+    g = load_golden(name)
+    nx, ny, mask = case["nx"], case["ny"], g["mask"]
+    s0, init = initial_state(case, g, "f32", None)
+    results = []
+    for variant in VARIANTS:
+        with gpu_lib.Solver(nx, ny, case["tau_f32"], case["fx"], case["fy"], mask,
+                            precision=form) as s:
+            s.set_variant(variant)
+            if case.get("open_x"):
+                s.set_inflow_outflow(case["u_in"])
+            if s0 is None:
+                s.init_equilibrium(*init)
+            else:
+                s.set_populations(s0)
+            s.run(case["steps"])
+            results.append(s.populations())
+    fluid = np.repeat(mask == 0, 9)
+    for variant, r in zip(VARIANTS, results):
+        assert np.array_equal(r[fluid], results[0][fluid]), f"variant {variant} differs"
+
+
+@pytest.fixture(scope="module")
+def poiseuille_ref(gpu_lib):
+    nx, ny, tau = 128, 66, 0.6
+    fx = float(gpu_lib.poiseuille_force(ny - 2, tau, 0.05, np.float64))
+    mask = gpu_lib.make_channel(nx, ny)
+    steps = 20000
+    ref = gpu_lib.accuracy.run_form(gpu_lib, nx, ny, mask, tau, fx, 0.0, steps, "fp64")
+    return (nx, ny, mask, tau, fx, steps), ref
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_poiseuille_velocity_error_against_fp64(gpu_lib, poiseuille_ref, form):
+    (nx, ny, mask, tau, fx, steps), ref = poiseuille_ref
+    r, _ = gpu_lib.accuracy.compare_forms(gpu_lib, nx, ny, mask, tau, fx, 0.0, steps, form,
+                                          reference=ref)
+    print(f"\npoiseuille {nx}x{ny} {steps} steps {form}: {r}")
+    assert r["u_max_fp64"] > 0.01
+    assert r["velocity_l2"] <= VELOCITY_L2_MAX[form], r
+    assert abs(r["mass_drift"]) < 1e-3, r
+
+
+@pytest.fixture(scope="module")
+def cylinder_ref(gpu_lib):
+    nx, ny, tau, fx = 1024, 256, 0.548, 1.5e-7
+    mask = gpu_lib.workloads.cylinder_wake(nx, ny)
+    steps, init = 4000, (1.0, 0.05, 0.0)
+    ref = gpu_lib.accuracy.run_form(gpu_lib, nx, ny, mask, tau, fx, 0.0, steps, "fp64", init)
+    return (nx, ny, mask, tau, fx, steps, init), ref
+
+
+@pytest.mark.parametrize("form", FORMS)
+def test_cylinder_velocity_error_against_fp64(gpu_lib, cylinder_ref, form):
+    (nx, ny, mask, tau, fx, steps, init), ref = cylinder_ref
+    r, _ = gpu_lib.accuracy.compare_forms(gpu_lib, nx, ny, mask, tau, fx, 0.0, steps, form,
+                                          init=init, reference=ref)
+    print(f"\ncylinder {nx}x{ny} {steps} steps {form}: {r}")
+    assert r["velocity_l2"] <= VELOCITY_L2_MAX[form], r
+    assert abs(r["mass_drift"]) < 1e-3, r
