@@ -18,6 +18,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <new>
 #include <string>
@@ -75,75 +76,93 @@ __global__ void adj_code_kernel(const uint32_t* __restrict__ mask, const AdjGeom
   }
 }
 
-// Forward intermediates of one cell.
-template <class T>
-struct CellFwd {
-  T y[kQ];
-  T drho, rho, kf, d, ux, uy, Fx, Fy, usq;
-  T cu[kQ], geq[kQ], guo[kQ], cf[kQ];
-  T alpha;
-};
-
-// Forward collision with Brinkman drag, the reference's operand order under policy A.
-template <class A>
-__device__ __forceinline__ void cell_forward(CellFwd<typename A::T>& f, const AdjParams<typename A::T>& p) {
+// Forward collision of one cell with Brinkman drag, the reference's operand order under policy A
+// (src/v0_cpu/solver_v0.cpp:127-143 with F replaced by F_tot): writes the 9 post-collision
+// values through `store(i, value)` one direction at a time, so that no per-direction array stays
+// live; returns u_x (the objective's integrand).
+template <class A, class Store>
+__device__ __forceinline__ typename A::T cell_forward(const typename A::T (&yv)[kQ], typename A::T alpha,
+                                                      const AdjParams<typename A::T>& p, Store&& store) {
   using T = typename A::T;
   T m0 = T(0), mx = T(0), my = T(0);
 #pragma unroll
   for (int i = 0; i < kQ; ++i) {
-    m0 = A::add(m0, f.y[i]);
-    mx = A::add(mx, A::mul(T(dir_cx(i)), f.y[i]));
-    my = A::add(my, A::mul(T(dir_cy(i)), f.y[i]));
+    m0 = A::add(m0, yv[i]);
+    mx = A::add(mx, A::mul(T(dir_cx(i)), yv[i]));
+    my = A::add(my, A::mul(T(dir_cy(i)), yv[i]));
   }
-  f.drho = m0;
-  f.rho = A::add(T(1), m0);
-  f.kf = A::add(T(1), A::mul(T(0.5), f.alpha));
-  f.d = A::mul(f.rho, f.kf);
-  f.ux = A::div(A::add(mx, p.hfx), f.d);
-  f.uy = A::div(A::add(my, p.hfy), f.d);
-  f.Fx = A::sub(p.fx, A::mul(A::mul(f.alpha, f.rho), f.ux));
-  f.Fy = A::sub(p.fy, A::mul(A::mul(f.alpha, f.rho), f.uy));
-  f.usq = A::add(A::mul(f.ux, f.ux), A::mul(f.uy, f.uy));
+  const T drho = m0;
+  const T rho = A::add(T(1), m0);
+  const T kf = A::add(T(1), A::mul(T(0.5), alpha));
+  const T d = A::mul(rho, kf);
+  const T ux = A::div(A::add(mx, p.hfx), d);
+  const T uy = A::div(A::add(my, p.hfy), d);
+  const T Fx = A::sub(p.fx, A::mul(A::mul(alpha, rho), ux));
+  const T Fy = A::sub(p.fy, A::mul(A::mul(alpha, rho), uy));
+  const T usq = A::add(A::mul(ux, ux), A::mul(uy, uy));
 #pragma unroll
   for (int i = 0; i < kQ; ++i) {
     const T cx = T(dir_cx(i)), cy = T(dir_cy(i)), w = weight<T>(i);
-    const T cu = A::add(A::mul(cx, f.ux), A::mul(cy, f.uy));
-    f.cu[i] = cu;
-    const T br = A::sub(A::add(A::mul(T(3), cu), A::mul(A::mul(T(4.5), cu), cu)), A::mul(T(1.5), f.usq));
-    f.geq[i] = A::mul(w, A::add(f.drho, A::mul(f.rho, br)));
-    const T cf = A::add(A::mul(cx, f.Fx), A::mul(cy, f.Fy));
-    f.cf[i] = cf;
-    const T tf = A::add(A::mul(A::sub(cx, f.ux), f.Fx), A::mul(A::sub(cy, f.uy), f.Fy));
-    f.guo[i] = A::mul(w, A::add(A::mul(T(3), tf), A::mul(A::mul(T(9), cu), cf)));
+    const T cu = A::add(A::mul(cx, ux), A::mul(cy, uy));
+    const T br = A::sub(A::add(A::mul(T(3), cu), A::mul(A::mul(T(4.5), cu), cu)), A::mul(T(1.5), usq));
+    const T geq = A::mul(w, A::add(drho, A::mul(rho, br)));
+    const T cf = A::add(A::mul(cx, Fx), A::mul(cy, Fy));
+    const T tf = A::add(A::mul(A::sub(cx, ux), Fx), A::mul(A::sub(cy, uy), Fy));
+    const T guo = A::mul(w, A::add(A::mul(T(3), tf), A::mul(A::mul(T(9), cu), cf)));
+    store(i, A::add(A::sub(yv[i], A::mul(p.omega, A::sub(yv[i], geq))), A::mul(p.fp, guo)));
   }
+  return ux;
 }
 
+// Periodic neighbourhood of cell (x, y): column of x - 1, x, x + 1 and row offset (times nx) of
+// y - 1, y, y + 1, so that every gather index is one add.
+struct Nbhd {
+  int col[3];
+  int row[3];
+};
+__device__ __forceinline__ Nbhd nbhd(const AdjGeom& g, int x, int y) {
+  Nbhd h;
+  h.col[0] = x == 0 ? g.nx - 1 : x - 1;
+  h.col[1] = x;
+  h.col[2] = x == g.nx - 1 ? 0 : x + 1;
+  h.row[0] = (y == 0 ? g.ny - 1 : y - 1) * g.nx;
+  h.row[1] = y * g.nx;
+  h.row[2] = (y == g.ny - 1 ? 0 : y + 1) * g.nx;
+  return h;
+}
+
+// Pull gather y = P R of one cell: y_i = solid(c - e_i) ? R[opp i][c] : R[i][c - e_i].
 template <class T>
-__device__ __forceinline__ void gather_fwd(const T* R, uint32_t code, const AdjGeom& g, int x,
-                                           int y, long long c, T (&out)[kQ]) {
+__device__ __forceinline__ void gather_fwd(const T* R, uint32_t code, const AdjGeom& g, const Nbhd& h,
+                                           int c, T (&out)[kQ]) {
 #pragma unroll
   for (int i = 0; i < kQ; ++i) {
-    if ((code >> i) & 1u) {
-      out[i] = R[dir_opp(i) * g.n + c];
-    } else {
-      out[i] = R[i * g.n + wrap_cell(g, x - dir_cx(i), y - dir_cy(i))];
-    }
+    const int src = ((code >> i) & 1u) ? c
+                                       : h.row[1 - dir_cy(i)] + h.col[1 - dir_cx(i)];
+    const int plane = ((code >> i) & 1u) ? dir_opp(i) : i;
+    out[i] = R[static_cast<long long>(plane) * g.n + src];
   }
 }
 
-// Transpose of the pull gather (closed domain).
+// Transpose of the pull gather (closed domain): (P^T Z)_j = solid(c + e_j) ? Z[opp j][c]
+// : Z[j][c + e_j].
 template <class T>
 __device__ __forceinline__ void gather_transpose(const T* Z, uint32_t code, const AdjGeom& g,
-                                                 int x, int y, long long c, T (&out)[kQ]) {
+                                                 const Nbhd& h, int c, T (&out)[kQ]) {
 #pragma unroll
   for (int j = 0; j < kQ; ++j) {
-    if ((code >> (9 + j)) & 1u) {
-      out[j] = Z[dir_opp(j) * g.n + c];
-    } else {
-      out[j] = Z[j * g.n + wrap_cell(g, x + dir_cx(j), y + dir_cy(j))];
-    }
+    const bool bounce = (code >> (9 + j)) & 1u;
+    const int src = bounce ? c : h.row[1 + dir_cy(j)] + h.col[1 + dir_cx(j)];
+    const int plane = bounce ? dir_opp(j) : j;
+    out[j] = Z[static_cast<long long>(plane) * g.n + src];
   }
 }
+
+// Reciprocal of the backward sweep's linearisation (rounding-level accuracy suffices there):
+// FP32 uses the hardware approximation, which keeps the IEEE division's out-of-line slow path
+// (and the register spills its call forces) out of the kernel.
+__device__ __forceinline__ float adj_rcp(float d) { return __fdividef(1.0f, d); }
+__device__ __forceinline__ double adj_rcp(double d) { return 1.0 / d; }
 
 __device__ __forceinline__ void block_add_to(double v, double* target, double* smem) {
 #pragma unroll
@@ -173,6 +192,7 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
   const T* Rb = R + b * g.inst;
   T* Rnb = Rn ? Rn + b * g.inst : nullptr;
   T usum = T(0);  // per-thread partial sum (a few cells), added in double per block below
+#pragma unroll 1
   for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < g.n;
        c += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int y = static_cast<int>(c / g.nx), x = static_cast<int>(c - static_cast<long long>(y) * g.nx);
@@ -184,17 +204,13 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
       }
       continue;
     }
-    CellFwd<T> f;
-    gather_fwd(Rb, code, g, x, y, c, f.y);
-    f.alpha = p.alpha ? p.alpha[b * g.n + c] : T(0);
-    cell_forward<A>(f, p);
-    if (obj) usum += f.ux;
-    if (write_out) {
-#pragma unroll
-      for (int i = 0; i < kQ; ++i)
-        Rnb[i * g.n + c] = A::add(A::sub(f.y[i], A::mul(p.omega, A::sub(f.y[i], f.geq[i]))),
-                                  A::mul(p.fp, f.guo[i]));
-    }
+    T yv[kQ];
+    gather_fwd(Rb, code, g, nbhd(g, x, y), static_cast<int>(c), yv);
+    const T alpha = p.alpha ? p.alpha[b * g.n + c] : T(0);
+    const T ux = cell_forward<A>(yv, alpha, p, [&](int i, T v) {
+      if (write_out) Rnb[i * g.n + c] = v;
+    });
+    if (obj) usum += ux;
   }
   if (obj) block_add_to(static_cast<double>(usum), obj + b, smem);
 }
@@ -219,6 +235,7 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
   const T* Yn = Ynext ? Ynext + b * g.inst : nullptr;
   T* Yb = Ybar + b * g.inst;
   T g_omega = T(0), g_fx = T(0), g_fy = T(0);  // per-thread partial sums (a few cells)
+#pragma unroll 1
   for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < g.n;
        c += static_cast<long long>(gridDim.x) * blockDim.x) {
     const int y = static_cast<int>(c / g.nx), x = static_cast<int>(c - static_cast<long long>(y) * g.nx);
@@ -228,62 +245,62 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
       for (int i = 0; i < kQ; ++i) Yb[i * g.n + c] = T(0);
       continue;
     }
+    const Nbhd h = nbhd(g, x, y);
     T yv[kQ];
-    gather_fwd(Rb, code, g, x, y, c, yv);
+    gather_fwd(Rb, code, g, h, static_cast<int>(c), yv);
     T v[kQ];
     if (Yn) {
-      gather_transpose(Yn, code, g, x, y, c, v);
+      gather_transpose(Yn, code, g, h, static_cast<int>(c), v);
     } else {
 #pragma unroll
       for (int i = 0; i < kQ; ++i) v[i] = T(0);
     }
-    // Forward intermediates (FMA arithmetic).
+    // Forward intermediates (FMA arithmetic; zero-coefficient terms dropped at compile time).
     const T alpha = p.alpha ? p.alpha[b * g.n + c] : T(0);
-    T drho = T(0), mx = T(0), my = T(0);
-#pragma unroll
-    for (int i = 0; i < kQ; ++i) {
-      drho += yv[i];
-      mx += T(dir_cx(i)) * yv[i];
-      my += T(dir_cy(i)) * yv[i];
-    }
+    const T drho = ((yv[0] + yv[1]) + (yv[2] + yv[3])) + ((yv[4] + yv[5]) + (yv[6] + yv[7])) + yv[8];
+    const T mx = (yv[1] - yv[3]) + (yv[5] - yv[6]) + (yv[8] - yv[7]);
+    const T my = (yv[2] - yv[4]) + (yv[5] + yv[6]) - (yv[7] + yv[8]);
     const T rho = T(1) + drho;
     const T kf = T(1) + T(0.5) * alpha;
     const T d = rho * kf;
-    const T inv_d = T(1) / d;
+    const T inv_d = adj_rcp(d);
     const T ux = (mx + p.hfx) * inv_d, uy = (my + p.hfy) * inv_d;
     const T Fx = p.fx - alpha * rho * ux, Fy = p.fy - alpha * rho * uy;
     const T usq = ux * ux + uy * uy;
-    // Backward through post_i = y_i - omega (y_i - geq_i) + fp guo_i.
-    T yb[kQ];
-    T d_drho = T(0), d_rho = T(0), d_ux = obj_coef, d_uy = T(0), d_usq = T(0);
-    T d_Fx = T(0), d_Fy = T(0), om = T(0);
+    // Backward through post_i = y_i - omega (y_i - geq_i) + fp guo_i in closed form: every sum
+    // over directions of v_i w_i times a polynomial in c_i is a weighted moment of v (c^3 = c for
+    // c in {0, +-1}):
+    //   V0 = sum w v, Vx = sum w v c_x, Vy, Vxx = sum w v c_x^2, Vxy = sum w v c_x c_y, Vyy.
+    const T D = (v[5] + v[6]) + (v[7] + v[8]);
+    const T a13 = v[1] + v[3], a24 = v[2] + v[4];
+    const T w1 = T(1) / T(9), w5 = T(1) / T(36);
+    const T V0 = T(4) / T(9) * v[0] + w1 * (a13 + a24) + w5 * D;
+    const T Vx = w1 * (v[1] - v[3]) + w5 * ((v[5] - v[6]) + (v[8] - v[7]));
+    const T Vy = w1 * (v[2] - v[4]) + w5 * ((v[5] + v[6]) - (v[7] + v[8]));
+    const T Vxx = w1 * a13 + w5 * D, Vyy = w1 * a24 + w5 * D;
+    const T Vxy = w5 * ((v[5] - v[6]) + (v[7] - v[8]));
+    T vy = T(0);  // sum v_i y_i
 #pragma unroll
-    for (int i = 0; i < kQ; ++i) {
-      const T cx = T(dir_cx(i)), cy = T(dir_cy(i)), w = weight<T>(i);
-      const T cu = cx * ux + cy * uy;
-      const T A_i = T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq;
-      const T geq = w * (drho + rho * A_i);
-      const T cf = cx * Fx + cy * Fy;
-      const T tf = (cx - ux) * Fx + (cy - uy) * Fy;
-      const T guo = w * (T(3) * tf + T(9) * cu * cf);
-      yb[i] = (T(1) - p.omega) * v[i];
-      om += v[i] * (geq - yv[i] - T(0.5) * guo);
-      const T wg = p.omega * v[i] * w;  // d/d(drho + rho A_i)
-      d_drho += wg;
-      d_rho += wg * A_i;
-      const T Ab = wg * rho;
-      const T wu = p.fp * v[i] * w;  // d/d(3 tf + 9 cu cf)
-      const T cub = Ab * (T(3) + T(9) * cu) + T(9) * wu * cf;
-      d_usq -= T(1.5) * Ab;
-      const T tfb = T(3) * wu;
-      const T cfb = T(9) * wu * cu;
-      d_ux += cub * cx - tfb * Fx;
-      d_uy += cub * cy - tfb * Fy;
-      d_Fx += tfb * (cx - ux) + cfb * cx;
-      d_Fy += tfb * (cy - uy) + cfb * cy;
-    }
-    d_ux += T(2) * ux * d_usq;
-    d_uy += T(2) * uy * d_usq;
+    for (int i = 0; i < kQ; ++i) vy += v[i] * yv[i];
+    const T uV = ux * Vx + uy * Vy;
+    const T Q = ux * ux * Vxx + T(2) * ux * uy * Vxy + uy * uy * Vyy;
+    const T sA = T(3) * uV + T(4.5) * Q - T(1.5) * usq * V0;  // sum w v A_i
+    const T cxu = ux * Vxx + uy * Vxy, cyu = ux * Vxy + uy * Vyy;  // sum w v cu c_x, c_y
+    const T cxF = Fx * Vxx + Fy * Vxy, cyF = Fx * Vxy + Fy * Vyy;  // sum w v cf c_x, c_y
+    const T sgeq = drho * V0 + rho * sA;                            // sum v geq
+    const T sguo = T(3) * (Fx * Vx + Fy * Vy - (ux * Fx + uy * Fy) * V0) +
+                   T(9) * (ux * cxF + uy * cyF);                     // sum v guo
+    const T om = sgeq - vy - T(0.5) * sguo;
+    const T orho = p.omega * rho;
+    T d_drho = p.omega * V0;
+    T d_rho = p.omega * sA;
+    const T d_usq = T(-1.5) * orho * V0;
+    T d_ux = obj_coef + orho * (T(3) * Vx + T(9) * cxu) + T(9) * p.fp * cxF - T(3) * p.fp * Fx * V0 +
+             T(2) * ux * d_usq;
+    T d_uy = orho * (T(3) * Vy + T(9) * cyu) + T(9) * p.fp * cyF - T(3) * p.fp * Fy * V0 +
+             T(2) * uy * d_usq;
+    const T d_Fx = T(3) * p.fp * (Vx - ux * V0) + T(9) * p.fp * cxu;
+    const T d_Fy = T(3) * p.fp * (Vy - uy * V0) + T(9) * p.fp * cyu;
     // F_tot = F - alpha rho u
     T a_b = -(d_Fx * rho * ux + d_Fy * rho * uy);
     d_rho -= alpha * (d_Fx * ux + d_Fy * uy);
@@ -296,9 +313,14 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
     a_b += T(0.5) * db * rho;
     // rho = 1 + drho, drho = sum y, m = sum c y
     const T dtot = d_drho + d_rho;
+    const T om1 = T(1) - p.omega;
 #pragma unroll
-    for (int i = 0; i < kQ; ++i)
-      Yb[i * g.n + c] = yb[i] + dtot + T(dir_cx(i)) * mxb + T(dir_cy(i)) * myb;
+    for (int i = 0; i < kQ; ++i) {
+      T o = om1 * v[i] + dtot;
+      if (dir_cx(i) != 0) o += dir_cx(i) > 0 ? mxb : -mxb;
+      if (dir_cy(i) != 0) o += dir_cy(i) > 0 ? myb : -myb;
+      Yb[i * g.n + c] = o;
+    }
     g_omega += om;
     g_fx += d_Fx + T(0.5) * mxb;
     g_fy += d_Fy + T(0.5) * myb;
@@ -352,7 +374,7 @@ __global__ void adj_get_state_kernel(const T* __restrict__ R, const uint32_t* __
 #pragma unroll
       for (int i = 0; i < kQ; ++i) s[i] = T(0);
     } else {
-      gather_fwd(R + b * g.inst, code, g, x, y, c, s);
+      gather_fwd(R + b * g.inst, code, g, nbhd(g, x, y), static_cast<int>(c), s);
     }
 #pragma unroll
     for (int i = 0; i < kQ; ++i) aos[c * kQ + i] = s[i];
@@ -433,9 +455,13 @@ AdjParams<T> params(const lbm_adjoint* a) {
   return p;
 }
 
+// Blocks per instance (grid x) and instances (grid y): about two waves of three resident blocks
+// per SM in total, so that each thread takes several cells and the per-block FP64 reductions of
+// the objective and the parameter gradients are amortised.
 dim3 grid2(const lbm_adjoint* a) {
   const long long want = (a->g.n + kAdjThreads - 1) / kAdjThreads;
-  const int bx = static_cast<int>(std::max<long long>(1, std::min<long long>(want, 8LL * a->sm_count)));
+  const long long target = (6LL * a->sm_count + a->batch - 1) / a->batch;
+  const int bx = static_cast<int>(std::max<long long>(1, std::min<long long>(want, target)));
   return dim3(bx, a->batch);
 }
 
@@ -587,7 +613,8 @@ int lbm_adj_create(int nx, int ny, const uint8_t* solid, double tau, double fx, 
   if (!out) return LBM_ERR_INVALID_ARG;
   *out = nullptr;
   if (nx < 1 || ny < 1 || !solid || batch < 1 || checkpoint_every < 1 || !(tau > 0.5) ||
-      (precision != LBM_FP32 && precision != LBM_FP64))
+      (precision != LBM_FP32 && precision != LBM_FP64) ||
+      static_cast<long long>(nx) * ny > static_cast<long long>(INT_MAX))  // 32-bit cell indices
     return LBM_ERR_INVALID_ARG;
   lbm_adjoint* a = new (std::nothrow) lbm_adjoint();
   if (!a) return LBM_ERR_OUT_OF_MEMORY;
