@@ -16,7 +16,10 @@ included (reference src/common/driver.hpp:120).
   roofline  HBM-bound: algorithmic bytes per cell update 2 * 9 * sizeof(float) = 72 B; achieved
             = 72 B * N / (average step-kernel duration); peak = measured copy bandwidth
             (MEASURED_PEAKS.json hbm_gbs); traffic = ncu DRAM bytes per launch (profiles/).
-  forms     the other forms on the same grid: FP64 (144 B/cell), FP16 and BF16 storage (36 B).
+  forms     the other forms on the same grid: FP64 (144 B/cell), FP16 and BF16 storage (36 B);
+            the 16-bit forms' velocity error and mass drift against FP64 (cylinder wake);
+            the adjoint's forward and backward step times (512 x 128 channel, batch of 32);
+            the batched ensemble (256 uneven channels) against one launch per instance.
   cpu_baseline  the oracle's OpenMP port of the reference's v1 solver on the host cores.
 
 --impl reference: the reference's CPU implementation of the path (the oracle's port of v1,
@@ -217,6 +220,31 @@ def accuracy_report(pkg):
     return out
 
 
+def batch_report(pkg, peak):
+    """Batched ensemble: 256 uneven closed channels (nx ~ U[64,1024], ny ~ U[32,512], 1-4 discs,
+    tau ~ U[0.52,1], fx ~ U[1e-6,1e-5], seed 7), autotuned, 640 steps as CUDA graphs of one
+    persistent launch per step, against the same instances stepped one launch per instance."""
+    specs = pkg.workloads.ensemble_specs(256, seed=7)
+    cells = sum(s["nx"] * s["ny"] for s in specs)
+    out = {"instances": len(specs), "cells": cells}
+    for prec in ("fp32", "fp16"):
+        try:
+            with pkg.Batch(specs, precision=prec) as b:
+                b.init_equilibrium(1.0, 0.0, 0.0)
+                tune = b.autotune()
+                b.run(64)
+                tb = b.timed_run(640)
+                ts = b.run_separate(64)
+            ml = cells * 640 / tb / 1e6
+            out[prec] = {"batched_mlups": round(ml, 1),
+                         "separate_mlups": round(cells * 64 / ts / 1e6, 1),
+                         "hbm_frac": round(BYTES_PER_CELL[prec] * ml * 1e6 / 1e9 / peak, 4),
+                         "autotune": tune.split(" | ")[0]}
+        except Exception as e:
+            out[prec] = {"error": str(e)[:200]}
+    return out
+
+
 def adjoint_report(pkg, peak):
     """Adjoint form on its workload (512 x 128 channel, Brinkman field, J = mean u_x over the
     last 100 of 2000 steps, checkpoints every 100 steps), a batch of 32 alpha fields in FP32:
@@ -341,6 +369,8 @@ def run_ours(args):
             forms["accuracy_vs_fp64"] = accuracy_report(pkg)
         if args.adjoint:
             forms["adjoint"] = adjoint_report(pkg, peak)
+        if args.batch:
+            forms["batch"] = batch_report(pkg, peak)
 
     cpu = None
     if rank == 0 and args.cpu_baseline:
@@ -450,6 +480,8 @@ def main():
                     help="skip the 16-bit forms' accuracy runs against FP64")
     ap.add_argument("--no-adjoint", dest="adjoint", action="store_false",
                     help="skip the adjoint form")
+    ap.add_argument("--no-batch", dest="batch", action="store_false",
+                    help="skip the batched ensemble form")
     args = ap.parse_args()
     if args.steps < 1:
         ap.error("--steps must be >= 1")

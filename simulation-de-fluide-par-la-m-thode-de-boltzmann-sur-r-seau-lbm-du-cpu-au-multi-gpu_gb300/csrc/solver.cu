@@ -177,7 +177,7 @@ int launch_tma_t(lbm_solver* s, int steps) {
   a.sc = s->sc;
   const int tpr = (s->nx + S::TW - 1) / S::TW;
   const int tiles = tpr * s->ny;
-  const auto kernel = pull_step_tma_kernel<ST, Phys, kOpen, kStages>;
+  const auto kernel = tma_step_kernel<ST, Phys, kOpen, kStages>;
   const size_t smem = tma_smem_bytes<ST>(kStages);
   LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
@@ -215,7 +215,7 @@ int launch_async_t(lbm_solver* s, int steps) {
   const Eq9<T> e = step_inlet_eq<ST>(s);
   for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
   a.sc = s->sc;
-  const auto kernel = pull_step_async_kernel<ST, Phys, kOpen, kDepth>;
+  const auto kernel = async_step_kernel<ST, Phys, kOpen, kDepth>;
   const size_t smem = async_smem_bytes<ST>(kDepth, kBlock / 32);
   LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                    static_cast<int>(smem)));
@@ -255,7 +255,7 @@ int launch_ring_t(lbm_solver* s, int steps) {
     a.sc = s->sc;
     const int tpr = (s->nx + S::TW - 1) / S::TW;
     const int tiles = tpr * s->ny;
-    const auto kernel = pull_step_ring_kernel<ST, Phys, kOpen, kW, kC, kStages, kMinBlocks>;
+    const auto kernel = ring_step_kernel<ST, Phys, kOpen, kW, kC, kStages, kMinBlocks>;
     const size_t smem = ring_smem_bytes<S>(kStages);
     LBM_CUDA(s, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      static_cast<int>(smem)));

@@ -1,5 +1,5 @@
 // Pull stream-collide step with a per-warp asynchronous-copy pipeline. Same results as
-// pull_step_kernel (step_kernel.cuh) and pull_step_tma_kernel (step_tma.cuh); different data path:
+// pull_step_kernel (step_kernel.cuh) and tma_step_kernel (step_tma.cuh); different data path:
 //
 //   * a warp owns chunks of 32 * G consecutive cells of one row (G cells per lane), taken
 //     grid-stride like the direct kernel;
@@ -93,7 +93,7 @@ __device__ __forceinline__ void issue_chunk(const StepArgs<ST, Phys>& p, unsigne
 }
 
 template <class ST, class Phys, bool kOpen, int kDepth>
-__global__ void __launch_bounds__(128) pull_step_async_kernel(const StepArgs<ST, Phys> p) {
+__global__ void __launch_bounds__(128) async_step_kernel(const StepArgs<ST, Phys> p) {
   using S = AsyncShape<ST>;
   extern __shared__ __align__(128) unsigned char smem[];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;

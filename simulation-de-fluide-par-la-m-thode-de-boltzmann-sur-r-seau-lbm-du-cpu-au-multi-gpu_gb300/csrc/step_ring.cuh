@@ -1,6 +1,6 @@
 // Warp-specialised pull stream-collide step, one cell (plain FP32 / FP64 storage) or one pair of
 // cells (16-bit storage) per lane.
-// Same results as pull_step_kernel (step_kernel.cuh); same producer as pull_step_tma_kernel
+// Same results as pull_step_kernel (step_kernel.cuh); same producer as tma_step_kernel
 // (step_tma.cuh), different consumers:
 //
 //   * a tile is TW = kW * 32 * kC consecutive cells of one row; the producer warp (one lane)
@@ -228,7 +228,7 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
 
 template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
-    pull_step_ring_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
+    ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
   using S = RingShape<ST, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);

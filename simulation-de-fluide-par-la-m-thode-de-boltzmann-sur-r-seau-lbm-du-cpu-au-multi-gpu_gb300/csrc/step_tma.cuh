@@ -273,7 +273,7 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
 
 template <class ST, class Phys, bool kOpen, int kStages>
 __global__ void __launch_bounds__(kTmaThreads, kStages <= 3 ? 2 : 1)
-    pull_step_tma_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
+    tma_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
   using S = TmaShape<ST>;
   extern __shared__ __align__(128) unsigned char smem[];
   // Stage s: 9 plane rows (kPlaneBytes) then 3 mask rows (3 * MW words).
