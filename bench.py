@@ -19,7 +19,8 @@ included (reference src/common/driver.hpp:120).
   forms     the other forms on the same grid: FP64 (144 B/cell), FP16 and BF16 storage (36 B);
             the 16-bit forms' velocity error and mass drift against FP64 (cylinder wake);
             the adjoint's forward and backward step times (512 x 128 channel, batch of 32);
-            the batched ensemble (256 uneven channels) against one launch per instance.
+            the batched ensemble (256 uneven channels) against one launch per instance;
+            the cylinder wake at Re 100 in every form (Strouhal number, lift, drag).
   cpu_baseline  the oracle's OpenMP port of the reference's v1 solver on the host cores.
 
 --impl reference: the reference's CPU implementation of the path (the oracle's port of v1,
@@ -137,7 +138,10 @@ class ClockSampler:
                 "power_w_median": statistics.median([num(r[2]) for r in inside if num(r[2])] or [0])}
 
 
-def dist_setup(n_gpus: int):
+def dist_setup(n_gpus: int, backend: str = "nccl"):
+    """Rank, local rank, world size and the process group (None for one process). Each rank
+    runs an independent replica of the workload; the group only carries the barrier and the
+    max-over-ranks of the timed region."""
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     local = int(os.environ.get("LOCAL_RANK", "0"))
@@ -145,7 +149,6 @@ def dist_setup(n_gpus: int):
     if world > 1:
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        backend = "nccl"
         dist.init_process_group(backend=backend)
     return rank, local, world, dist
 
@@ -159,7 +162,8 @@ def max_over_ranks(x: float, dist) -> float:
     if dist is None:
         return x
     import torch
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    device = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=device)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
@@ -217,6 +221,32 @@ def accuracy_report(pkg):
                      if k != "form"}
     out["workload"] = (f"cylinder wake {nx}x{ny}, disc D=32 at (256,129), tau {tau}, "
                        f"F=({fx},0), start u=(0.05,0), {steps} steps, stochastic rounding")
+    return out
+
+
+def wake_report(pkg):
+    """Cylinder wake at Re 100 (1024 x 256, disc D = 32, tau 0.548, calibrated body force, start
+    u = (0.05, 0)), 200k steps in every form: Strouhal number from the lift on the disc
+    (momentum exchange on the device, sampled every 50 steps), lift rms and mean drag over the
+    second half, against the FP64 run."""
+    out = {}
+    for prec in ("fp64", "fp32", "fp16", "bf16"):
+        try:
+            t0 = time.perf_counter()
+            s = pkg.wake.lift_series(pkg, prec, steps=200_000, every=50)
+            r = pkg.wake.strouhal(s)
+            out[prec] = {"st": round(r["st"], 5), "lift_rms": round(r["lift_rms"], 6),
+                         "drag_mean": round(r["drag_mean"], 6), "u_bulk": round(s["u_bulk"], 6),
+                         "finite": bool(s["finite"]), "wall_s": round(time.perf_counter() - t0, 2)}
+        except Exception as e:
+            out[prec] = {"error": str(e)[:200]}
+    if "st" in out.get("fp64", {}):
+        for prec in ("fp32", "fp16", "bf16"):
+            if "st" in out.get(prec, {}):
+                out[prec]["st_rel_diff_vs_fp64"] = round(out[prec]["st"] / out["fp64"]["st"] - 1.0, 5)
+    out["workload"] = ("cylinder wake 1024x256, disc D=32 at (256,129), tau 0.548, Re 100, "
+                       f"F=({pkg.wake.WAKE_FORCE:.4g},0) calibrated for u_bulk 0.05, 200k steps, "
+                       "lift sampled every 50 steps")
     return out
 
 
@@ -371,6 +401,8 @@ def run_ours(args):
             forms["adjoint"] = adjoint_report(pkg, peak)
         if args.batch:
             forms["batch"] = batch_report(pkg, peak)
+        if args.wake:
+            forms["cylinder_wake"] = wake_report(pkg)
 
     cpu = None
     if rank == 0 and args.cpu_baseline:
@@ -482,6 +514,8 @@ def main():
                     help="skip the adjoint form")
     ap.add_argument("--no-batch", dest="batch", action="store_false",
                     help="skip the batched ensemble form")
+    ap.add_argument("--no-wake", dest="wake", action="store_false",
+                    help="skip the cylinder-wake comparison of the forms")
     args = ap.parse_args()
     if args.steps < 1:
         ap.error("--steps must be >= 1")

@@ -130,6 +130,17 @@ int lbm_total_mass(lbm_solver* s, double* mass);
  * populations of cell (x, y) into out9 (host type). */
 int lbm_populations_at(lbm_solver* s, int x, int y, void* out9);
 
+/* Body force by momentum exchange (no counterpart in the reference, which computes no lift;
+ * its cylinder case probes u_y behind the disc, src/common/driver.hpp:167-184). For halfway
+ * bounce-back on stationary walls, every link from a fluid cell x to a body cell x + c_i carries
+ * 2 c_i f*_i(x), f*_i the post-collision population of x leaving along c_i; lbm_body_force sums
+ * them over the current state in FP64 (lattice units: force per unit depth). The body is a
+ * subset of the solid cells (nx*ny bytes, row-major, nonzero = body) set with lbm_set_body;
+ * a null body (the default) means every solid cell. Links leaving an open x boundary carry
+ * nothing. */
+int lbm_set_body(lbm_solver* s, const uint8_t* body);
+int lbm_body_force(lbm_solver* s, double* fx, double* fy);
+
 /* Writes 1 to *finite if every population is finite, else 0 (device check). */
 int lbm_check_finite(lbm_solver* s, int* finite);
 

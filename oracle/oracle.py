@@ -196,6 +196,37 @@ def total_mass(nx, ny, solid, s, real="f32") -> float:
                                          np.ascontiguousarray(s, _dtype(real)).reshape(-1))
 
 
+CX = np.array([0, 1, 0, -1, 0, 1, -1, -1, 1])
+CY = np.array([0, 0, 1, 0, -1, 1, 1, -1, -1])
+OPP = np.array([0, 3, 4, 1, 2, 7, 8, 5, 6])
+W = np.array([4 / 9] + [1 / 9] * 4 + [1 / 36] * 4)
+
+
+def body_force(nx, ny, solid, body, s, open_x=False):
+    """Momentum-exchange force on `body` from a v0 post-streaming state S, in FP64 (numpy).
+
+    Halfway bounce-back on stationary walls: a fluid cell x whose neighbour x + c_i is a body
+    cell sends f*_i(x) (post-collision) into the wall and receives it back as S_opp(i)(x), so the
+    link carries 2 c_i f*_i(x) = 2 c_i (S_opp(i)(x) + w_i) in the shifted variables. Written from
+    the method (the reference computes no force); the solver's device sum is checked against it.
+    Links leaving an open x boundary carry nothing."""
+    solid = np.asarray(solid, bool).reshape(ny, nx)
+    body = np.asarray(body, bool).reshape(ny, nx)
+    st = np.asarray(s, np.float64).reshape(ny, nx, 9)
+    fx = fy = 0.0
+    ys, xs = np.mgrid[0:ny, 0:nx]
+    fluid = ~solid
+    for i in range(1, 9):
+        xn, yn = xs + CX[i], (ys + CY[i]) % ny
+        inside = (xn >= 0) & (xn < nx) if open_x else np.ones_like(fluid)
+        xn = xn % nx
+        link = fluid & inside & body[yn, xn]
+        f = st[..., OPP[i]][link] + W[i]
+        fx += 2.0 * CX[i] * f.sum()
+        fy += 2.0 * CY[i] * f.sum()
+    return fx, fy
+
+
 def max_threads() -> int:
     return lib().lib.oracle_max_threads()
 

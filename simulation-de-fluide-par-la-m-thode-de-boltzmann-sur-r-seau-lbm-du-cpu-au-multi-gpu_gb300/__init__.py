@@ -17,7 +17,7 @@ from pathlib import Path
 
 import numpy as np
 
-from . import accuracy, geometry, workloads  # noqa: F401  (re-exported)
+from . import accuracy, geometry, wake, workloads  # noqa: F401  (re-exported)
 from .geometry import make_channel, make_cylinder, poiseuille_force  # noqa: F401
 
 _HERE = Path(__file__).resolve().parent
@@ -69,6 +69,8 @@ def lib() -> C.CDLL:
             "lbm_get_shape": ([vp, C.POINTER(i), C.POINTER(i), C.POINTER(i)], i),
             "lbm_set_launch": ([vp, i, i], i),
             "lbm_set_variant": ([vp, i], i),
+            "lbm_set_body": ([vp, vp], i),
+            "lbm_body_force": ([vp, C.POINTER(d), C.POINTER(d)], i),
             "lbm_state_view": ([vp, C.POINTER(vp), C.POINTER(C.c_longlong), C.POINTER(i)], i),
             "lbm_adj_create": ([i, i, vp, d, d, d, i, i, i, C.POINTER(vp)], i),
             "lbm_adj_destroy": ([vp], i),
@@ -121,7 +123,7 @@ class Solver:
     """D2Q9 BGK + Guo + halfway bounce-back solver on one GPU (drop-in for lbm::SolverV3).
 
     precision: "fp32" / "fp64" (bit-exact with the reference's v0 in float / double),
-    "fp16" / "bf16" (16-bit storage of g_i with per-plane scales, FP32 arithmetic).
+    "fp16" / "bf16" (16-bit storage of 2^15 g_i with stochastic rounding, FP32 arithmetic).
     Host arrays use the reference's v0 layout and the solver's host dtype (float32, or float64
     for "fp64").
     """
@@ -233,6 +235,24 @@ class Solver:
 
     def set_variant(self, variant: int):
         self._check(lib().lbm_set_variant(self._h, variant))
+
+    def set_body(self, body=None):
+        """Cells whose momentum-exchange force body_force() sums (a subset of the solid cells;
+        None: every solid cell)."""
+        if body is None:
+            self._check(lib().lbm_set_body(self._h, None))
+            return
+        b = np.ascontiguousarray(body, dtype=np.uint8).reshape(-1)
+        if b.size != self._nx * self._ny:
+            raise ValueError("body must hold nx*ny values")
+        self._body = b
+        self._check(lib().lbm_set_body(self._h, _ptr(b)))
+
+    def body_force(self):
+        """(F_x, F_y) on the body by momentum exchange, FP64, lattice units."""
+        fx, fy = C.c_double(), C.c_double()
+        self._check(lib().lbm_body_force(self._h, C.byref(fx), C.byref(fy)))
+        return fx.value, fy.value
 
     def set_stream(self, stream_handle: int):
         self._check(lib().lbm_set_stream(self._h, C.c_void_p(stream_handle)))

@@ -196,6 +196,61 @@ __global__ void finite_kernel(const ST* __restrict__ R, const uint32_t* __restri
   }
 }
 
+// Momentum-exchange force on a body (halfway bounce-back, stationary walls): every link from a
+// fluid cell x to a body cell x + c_i carries 2 c_i f*_i(x), with f*_i(x) = R_i(x) + w_i the
+// post-collision population of x leaving along c_i (the pull state holds post-collision
+// values), which bounces back unchanged. Links leaving an open x boundary carry nothing. FP64
+// per-block partials of (F_x, F_y).
+template <class ST>
+__global__ void __launch_bounds__(kReduceThreads)
+    body_force_partial_kernel(const ST* __restrict__ R, const uint32_t* __restrict__ mask,
+                              const uint32_t* __restrict__ body, const Grid2D g,
+                              const PlaneScales sc, double* __restrict__ partials) {
+  __shared__ double smem[32];
+  double ax = 0.0, ay = 0.0;
+  const long long n = static_cast<long long>(g.nx) * g.ny;
+  for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < n;
+       c += static_cast<long long>(gridDim.x) * blockDim.x) {
+    const int y = static_cast<int>(c / g.nx), x = static_cast<int>(c - static_cast<long long>(y) * g.nx);
+    if (mask_solid(mask, g.mask_words, x, y)) continue;
+#pragma unroll
+    for (int i = 1; i < kQ; ++i) {
+      int xn = x + dir_cx(i), yn = y + dir_cy(i);
+      if (g.open_x && (xn < 0 || xn >= g.nx)) continue;
+      xn = xn < 0 ? g.nx - 1 : (xn >= g.nx ? 0 : xn);
+      yn = yn < 0 ? g.ny - 1 : (yn >= g.ny ? 0 : yn);
+      if (!mask_solid(body, g.mask_words, xn, yn)) continue;
+      const double f = static_cast<double>(load_one<ST>(R + i * g.plane + cell_index(g, x, y), i, sc)) +
+                       weight<double>(i);
+      ax += 2.0 * dir_cx(i) * f;
+      ay += 2.0 * dir_cy(i) * f;
+    }
+  }
+  const double bx = block_sum(ax, smem);
+  const double by = block_sum(ay, smem);
+  if (threadIdx.x == 0) {
+    partials[2 * blockIdx.x] = bx;
+    partials[2 * blockIdx.x + 1] = by;
+  }
+}
+
+// Sum of `count` (x, y) partial pairs into out[0..1].
+static __global__ void __launch_bounds__(kReduceThreads)
+    pair_final_kernel(const double* __restrict__ partials, int count, double* __restrict__ out) {
+  __shared__ double smem[32];
+  double ax = 0.0, ay = 0.0;
+  for (int k = threadIdx.x; k < count; k += blockDim.x) {
+    ax += partials[2 * k];
+    ay += partials[2 * k + 1];
+  }
+  const double bx = block_sum(ax, smem);
+  const double by = block_sum(ay, smem);
+  if (threadIdx.x == 0) {
+    out[0] = bx;
+    out[1] = by;
+  }
+}
+
 // Gather of one cell (velocity probe).
 template <class ST>
 __global__ void probe_kernel(const ST* __restrict__ R, const uint32_t* __restrict__ mask,

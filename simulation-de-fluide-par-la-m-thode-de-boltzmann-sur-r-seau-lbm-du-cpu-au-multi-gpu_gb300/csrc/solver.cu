@@ -380,6 +380,18 @@ int finite_t(lbm_solver* s, int* flag) {
 }
 
 template <class ST>
+int body_force_t(lbm_solver* s, double* out) {
+  const long long n = static_cast<long long>(s->nx) * s->ny;
+  const uint32_t* body = s->body_d ? s->body_d : s->mask_d;
+  body_force_partial_kernel<ST><<<s->red_blocks, kReduceThreads, 0, s->stream>>>(
+      static_cast<const ST*>(s->buf[s->cur]), s->mask_d, body, s->g, s->sc, s->force_red);
+  pair_final_kernel<<<1, kReduceThreads, 0, s->stream>>>(s->force_red, s->red_blocks, out);
+  (void)n;
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
+}
+
+template <class ST>
 int probe_t(lbm_solver* s, int x, int y, void* out) {
   using T = typename StoreTraits<ST>::T;
   probe_kernel<ST><<<1, 32, 0, s->stream>>>(static_cast<const ST*>(s->buf[s->cur]), s->mask_d,
@@ -420,10 +432,9 @@ int ensure_stage(lbm_solver* s, size_t bytes) {
 
 int check(const lbm_solver* s) { return s ? LBM_OK : LBM_ERR_INVALID_ARG; }
 
-// Per-plane power-of-two scales of the 16-bit forms: the largest stored magnitude 65504 / scale
-// is 2 for the rest population, 0.5 for the axis and 0.25 for the diagonal ones, which holds
-// g_i = w_i [drho + rho (3 cu + 4.5 cu^2 - 1.5 u^2)] for |u| <= 0.3 and |drho| <= 0.5 with the
-// smallest values of interest (~1e-9) still above the FP16 subnormal range.
+// Storage scales: 1 for the plain forms, kStoreScale16 (2^15) on every plane of the 16-bit forms
+// (the largest stored magnitude 65504 / 2^15 ~ 2 bounds |g_i| = |f_i - w_i| of any state with
+// 0 <= f_i <= 1, and values down to 2^-29 stay normal).
 PlaneScales default_scales(int precision) {
   PlaneScales p{};
   const bool s16 = precision == LBM_FP16_STORE || precision == LBM_BF16_STORE;
@@ -570,6 +581,8 @@ int lbm_destroy(lbm_solver* s) {
   for (void* p : s->buf) cudaFree(p);
   cudaFree(s->mask_d);
   cudaFree(s->red);
+  cudaFree(s->body_d);
+  cudaFree(s->force_red);
   cudaFree(s->stage);
   for (cudaEvent_t ev : s->ev)
     if (ev) cudaEventDestroy(ev);
@@ -730,6 +743,46 @@ int lbm_populations_at(lbm_solver* s, int x, int y, void* out9) {
   if (rc) return rc;
   LBM_CUDA(s, cudaMemcpyAsync(out9, s->stage, kQ * s->host_elem, cudaMemcpyDeviceToHost, s->stream));
   LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_set_body(lbm_solver* s, const uint8_t* body) {
+  if (check(s)) return LBM_ERR_INVALID_ARG;
+  if (!body) {
+    cudaFree(s->body_d);
+    s->body_d = nullptr;
+    return LBM_OK;
+  }
+  const size_t n = static_cast<size_t>(s->nx) * s->ny;
+  for (size_t c = 0; c < n; ++c)
+    if (body[c] && !s->solid[c]) return set_error(s, LBM_ERR_INVALID_ARG, "body cells must be solid");
+  std::vector<uint32_t> words;
+  pack_mask(body, s->nx, s->ny, s->g.mask_words, words);
+  const size_t bytes = words.size() * sizeof(uint32_t);
+  if (!s->body_d) LBM_CUDA(s, cudaMalloc(&s->body_d, bytes));
+  LBM_CUDA(s, cudaMemcpyAsync(s->body_d, words.data(), bytes, cudaMemcpyHostToDevice, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  return LBM_OK;
+}
+
+int lbm_body_force(lbm_solver* s, double* fx, double* fy) {
+  if (check(s) || !fx || !fy) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
+  if (!s->force_red) LBM_CUDA(s, cudaMalloc(&s->force_red, (2 * s->red_blocks + 2) * sizeof(double)));
+  double* out = s->force_red + 2 * s->red_blocks;
+  int rc;
+  switch (s->precision) {
+    case LBM_FP32: rc = body_force_t<float>(s, out); break;
+    case LBM_FP64: rc = body_force_t<double>(s, out); break;
+    case LBM_FP16_STORE: rc = body_force_t<__half>(s, out); break;
+    case LBM_BF16_STORE: rc = body_force_t<__nv_bfloat16>(s, out); break;
+    default: rc = LBM_ERR_INVALID_ARG;
+  }
+  if (rc) return rc;
+  double f[2];
+  LBM_CUDA(s, cudaMemcpyAsync(f, out, sizeof(f), cudaMemcpyDeviceToHost, s->stream));
+  LBM_CUDA(s, cudaStreamSynchronize(s->stream));
+  *fx = f[0];
+  *fy = f[1];
   return LBM_OK;
 }
 

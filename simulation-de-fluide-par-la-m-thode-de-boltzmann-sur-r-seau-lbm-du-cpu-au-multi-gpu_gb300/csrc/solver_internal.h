@@ -20,6 +20,8 @@ struct lbm_solver {
   uint32_t t = 0;  // lattice steps taken (stochastic-rounding key of the 16-bit forms)
   size_t state_bytes = 0;
   uint32_t* mask_d = nullptr;  // bit-packed mask with periodic ghost bits
+  uint32_t* body_d = nullptr;  // bit-packed body of lbm_body_force (null: every solid cell)
+  double* force_red = nullptr;  // body-force partials [2 red_blocks], then the result pair
   std::vector<uint8_t> solid;  // host copy (the reference's solid())
   long long fluid = 0;
   double tau = 0, fx = 0, fy = 0;

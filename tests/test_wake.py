@@ -1,0 +1,41 @@
+"""Cylinder wake: the Strouhal estimator on synthetic series (CPU) and the wake itself on the
+GPU (FP32 against FP16, against the expected range at Re 100)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+
+def _series(period, amp=0.05, noise=0.0, n=4000, every=50, seed=0):
+    t = np.arange(1, n + 1) * float(every)
+    y = amp * np.sin(2 * np.pi * t / period) + 0.01
+    if noise:
+        y = y + noise * np.random.default_rng(seed).normal(size=n)
+    return {"t": t, "lift": y, "drag": np.full(n, 0.1), "u_bulk": 0.05, "d": 32.0}
+
+
+@pytest.mark.parametrize("period,noise", [(2861.9, 0.0), (2861.9, 0.01), (1500.0, 0.005), (6400.0, 0.0)])
+def test_strouhal_of_a_sine(pkg, period, noise):
+    r = pkg.wake.strouhal(_series(period, noise=noise))
+    assert r["st"] == pytest.approx(32.0 / period / 0.05, rel=2e-3)
+    assert r["drag_mean"] == pytest.approx(0.1)
+
+
+def test_wake_force_formula(pkg):
+    nu = (0.548 - 0.5) / 3.0
+    assert pkg.wake.wake_force() == pytest.approx(12 * nu * 0.05 / 254 ** 2)
+    solid, disc = pkg.wake.geometry()
+    assert disc.sum() > 700 and np.all(solid[disc == 1] == 1)
+
+
+@pytest.mark.gpu
+def test_wake_fp16_tracks_fp32(gpu_lib):
+    a = gpu_lib.wake.lift_series(gpu_lib, "fp32", steps=200_000, every=50)
+    b = gpu_lib.wake.lift_series(gpu_lib, "fp16", steps=200_000, every=50)
+    ra, rb = gpu_lib.wake.strouhal(a), gpu_lib.wake.strouhal(b)
+    print(f"\nwake fp32 {ra}\nwake fp16 {rb}")
+    assert a["finite"] and b["finite"]
+    assert a["u_bulk"] == pytest.approx(0.05, rel=0.03)
+    assert 0.20 < ra["st"] < 0.25
+    assert rb["st"] == pytest.approx(ra["st"], rel=0.02)
+    assert rb["drag_mean"] == pytest.approx(ra["drag_mean"], rel=0.03)
