@@ -196,6 +196,10 @@ __global__ void finite_kernel(const ST* __restrict__ R, const uint32_t* __restri
   }
 }
 
+// Advances the solver's device step counter (the stochastic-rounding key) after a launch
+// sequence, inside a captured graph as well.
+static __global__ void counter_add_kernel(uint32_t* c, uint32_t n) { *c += n; }
+
 // Momentum-exchange force on a body (halfway bounce-back, stationary walls): every link from a
 // fluid cell x to a body cell x + c_i carries 2 c_i f*_i(x), with f*_i(x) = R_i(x) + w_i the
 // post-collision population of x leaving along c_i (the pull state holds post-collision

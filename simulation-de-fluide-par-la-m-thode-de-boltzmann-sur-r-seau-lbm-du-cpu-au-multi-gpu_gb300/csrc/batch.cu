@@ -69,7 +69,6 @@ __global__ void __launch_bounds__(kBatchThreads)
   __shared__ int s_item0[kBatchMaxInstances];
   for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_item0[k] = a.inst[k].item0;
   __syncthreads();
-  const uint32_t rkey = sr_step_key(*a.step);
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   for (int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; item < a.items; item += nwarps) {
@@ -91,7 +90,8 @@ __global__ void __launch_bounds__(kBatchThreads)
     p.items = d.cpr * d.g.ny;
     p.k = d.k;
     p.sc = a.sc;
-    p.rkey = rkey;
+    p.step_ctr = a.step;
+    p.step_off = 0;
     p.key_base = d.off / kQ;
     const Chunk c = chunk_at<G>(item - d.item0, d.cpr, d.g.nx, d.g.ny, lane);
     T v[kQ][G];
@@ -322,6 +322,8 @@ int separate_t(lbm_batch* b, int steps) {
     a.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
     a.sc = b->sc;
     a.key_base = in.off / kQ;
+    a.step_ctr = b->step_d;
+    a.step_off = 0;
     grids[k] = std::max(1, std::min((a.items + kStepThreads / 32 - 1) / (kStepThreads / 32),
                                     std::max(1, per_sm) * b->sm_count));
   }
@@ -331,7 +333,6 @@ int separate_t(lbm_batch* b, int steps) {
     for (int k = 0; k < b->count; ++k) {
       args[k].src = src + b->inst[k].off;
       args[k].dst = dst + b->inst[k].off;
-      args[k].rkey = sr_step_key(b->t);
       kernel<<<grids[k], kStepThreads, 0, b->stream>>>(args[k]);
     }
     step_counter_add<<<1, 1, 0, b->stream>>>(b->step_d);

@@ -498,7 +498,7 @@ struct StepStore {
   static constexpr int kPairs = kSr ? G / 2 : 1;
   static __device__ __forceinline__ void hashes(long long cell0, uint32_t rkey, uint32_t (&ph)[kPairs]) {
 #pragma unroll
-    for (int k = 0; k < kPairs; ++k) ph[k] = kSr ? sr_pair_hash(cell0 + 2 * k, rkey) : 0u;
+    for (int k = 0; k < kPairs; ++k) ph[k] = sr_pair_hash(cell0 + 2 * k, rkey);
   }
   static __device__ __forceinline__ void store(ST* p, const typename StoreTraits<ST>::T (&v)[G], int i,
                                                const PlaneScales& s, const uint32_t (&ph)[kPairs]) {

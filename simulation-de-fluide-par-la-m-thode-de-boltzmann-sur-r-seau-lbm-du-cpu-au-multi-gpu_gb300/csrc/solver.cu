@@ -152,7 +152,8 @@ int launch_steps_t(lbm_solver* s, int steps) {
   for (int k = 0; k < steps; ++k) {
     a.src = static_cast<const ST*>(s->buf[s->cur]);
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
-    a.rkey = sr_step_key(s->t++);
+    a.step_ctr = s->step_ctr;
+    a.step_off = static_cast<uint32_t>(k);
     kernel<<<grid, s->block, 0, s->stream>>>(a);
     s->cur ^= 1;
   }
@@ -191,7 +192,8 @@ int launch_tma_t(lbm_solver* s, int steps) {
   for (int k = 0; k < steps; ++k) {
     a.src = static_cast<const ST*>(s->buf[s->cur]);
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
-    a.rkey = sr_step_key(s->t++);
+    a.step_ctr = s->step_ctr;
+    a.step_off = static_cast<uint32_t>(k);
     kernel<<<grid, kTmaThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
     s->cur ^= 1;
   }
@@ -230,7 +232,8 @@ int launch_async_t(lbm_solver* s, int steps) {
   for (int k = 0; k < steps; ++k) {
     a.src = static_cast<const ST*>(s->buf[s->cur]);
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
-    a.rkey = sr_step_key(s->t++);
+    a.step_ctr = s->step_ctr;
+    a.step_off = static_cast<uint32_t>(k);
     kernel<<<grid, kBlock, smem, s->stream>>>(a);
     s->cur ^= 1;
   }
@@ -269,7 +272,8 @@ int launch_ring_t(lbm_solver* s, int steps) {
     for (int k = 0; k < steps; ++k) {
       a.src = static_cast<const ST*>(s->buf[s->cur]);
       a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
-      a.rkey = sr_step_key(s->t++);
+      a.step_ctr = s->step_ctr;
+      a.step_off = static_cast<uint32_t>(k);
       kernel<<<grid, S::kThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
       s->cur ^= 1;
     }
@@ -319,7 +323,11 @@ int launch_steps_o(lbm_solver* s, int steps) {
 
 template <class ST>
 int launch_steps(lbm_solver* s, int steps) {
-  return s->open_x ? launch_steps_o<ST, true>(s, steps) : launch_steps_o<ST, false>(s, steps);
+  const int rc = s->open_x ? launch_steps_o<ST, true>(s, steps) : launch_steps_o<ST, false>(s, steps);
+  if (rc) return rc;
+  counter_add_kernel<<<1, 1, 0, s->stream>>>(s->step_ctr, static_cast<uint32_t>(steps));
+  LBM_CUDA(s, cudaGetLastError());
+  return LBM_OK;
 }
 
 template <class ST>
@@ -452,7 +460,60 @@ PlaneScales default_scales(int precision) {
 // ----------------------------------------------------------------------------------------------
 namespace lbm_b200 {
 
-int solver_step_raw(lbm_solver* s, int steps) { LBM_DISPATCH(s, launch_steps, s, steps); }
+int solver_launch(lbm_solver* s, int steps) { LBM_DISPATCH(s, launch_steps, s, steps); }
+
+void drop_step_graph(lbm_solver* s) {
+  if (s->graph) cudaGraphExecDestroy(s->graph);
+  s->graph = nullptr;
+  s->graph_cur = -1;
+}
+
+// Captures kGraphSteps step launches (and the step-counter update) from the current buffer
+// parity into a CUDA graph. kGraphSteps is even, so a replay leaves the parity unchanged. A
+// capture that fails turns graphs off for this solver (direct launches give the same results).
+int ensure_step_graph(lbm_solver* s) {
+  if (s->graph && s->graph_cur == s->cur) return LBM_OK;
+  drop_step_graph(s);
+  const int cur0 = s->cur;
+  cudaGraph_t g = nullptr;
+  if (cudaStreamBeginCapture(s->stream, cudaStreamCaptureModeRelaxed) != cudaSuccess) {
+    cudaGetLastError();
+    s->graphs = false;
+    return LBM_OK;
+  }
+  const int rc = solver_launch(s, kGraphSteps);
+  const cudaError_t e = cudaStreamEndCapture(s->stream, &g);
+  s->cur = cur0;
+  if (rc || e != cudaSuccess || !g) {
+    if (g) cudaGraphDestroy(g);
+    cudaGetLastError();
+    s->graphs = false;
+    return LBM_OK;
+  }
+  const cudaError_t ei = cudaGraphInstantiate(&s->graph, g, 0);
+  cudaGraphDestroy(g);
+  if (ei != cudaSuccess) {
+    cudaGetLastError();
+    s->graph = nullptr;
+    s->graphs = false;
+    return LBM_OK;
+  }
+  s->graph_cur = cur0;
+  return LBM_OK;
+}
+
+// Steps: whole CUDA graphs of kGraphSteps launches for long runs on a non-default stream (no
+// per-launch host overhead, which dominates small grids), direct launches for the remainder.
+int solver_step_raw(lbm_solver* s, int steps) {
+  if (s->graphs && s->stream != nullptr && steps >= kGraphSteps) {
+    if (int rc = ensure_step_graph(s)) return rc;
+    while (s->graph && steps >= kGraphSteps) {
+      LBM_CUDA(s, cudaGraphLaunch(s->graph, s->stream));
+      steps -= kGraphSteps;
+    }
+  }
+  return steps > 0 ? solver_launch(s, steps) : LBM_OK;
+}
 
 int solver_mass_into(lbm_solver* s, const void* state, double* partials, int blocks,
                      double* out) {
@@ -565,9 +626,10 @@ int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, doub
                         cudaMemcpyHostToDevice, s->stream);
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
   s->red_blocks = 4 * s->sm_count;
-  e = cudaMalloc(&s->red, (s->red_blocks + 2) * sizeof(double) + 2 * sizeof(int));
-  if (e == cudaSuccess) e = cudaMemsetAsync(s->red, 0, (s->red_blocks + 2) * sizeof(double) + 2 * sizeof(int), s->stream);
+  e = cudaMalloc(&s->red, (s->red_blocks + 2) * sizeof(double) + 4 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(s->red, 0, (s->red_blocks + 2) * sizeof(double) + 4 * sizeof(int), s->stream);
   s->err_flag = reinterpret_cast<int*>(s->red + s->red_blocks + 2) + 1;
+  s->step_ctr = reinterpret_cast<uint32_t*>(s->red + s->red_blocks + 2) + 2;
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
   e = cudaStreamSynchronize(s->stream);
   if (e != cudaSuccess) return fail(LBM_ERR_CUDA);
@@ -580,6 +642,7 @@ int lbm_destroy(lbm_solver* s) {
   if (s->stream) cudaStreamSynchronize(s->stream);
   for (void* p : s->buf) cudaFree(p);
   cudaFree(s->mask_d);
+  lbm_b200::drop_step_graph(s);
   cudaFree(s->red);
   cudaFree(s->body_d);
   cudaFree(s->force_red);
@@ -609,6 +672,7 @@ int lbm_set_inflow_outflow(lbm_solver* s, double u_in) {
   s->open_x = true;
   s->u_in = u_in;
   s->g.open_x = 1;
+  lbm_b200::drop_step_graph(s);
   return LBM_OK;
 }
 
@@ -843,6 +907,7 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
     return set_error(s, LBM_ERR_INVALID_ARG, "block must be a multiple of 32 and <= 256");
   s->block = block_threads;
   s->grid = grid_blocks;
+  lbm_b200::drop_step_graph(s);
   return LBM_OK;
 }
 
@@ -851,6 +916,7 @@ int lbm_set_variant(lbm_solver* s, int variant) {
   if (variant < -1 || variant > 17)
     return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 17]");
   s->variant = variant;
+  lbm_b200::drop_step_graph(s);
   return LBM_OK;
 }
 

@@ -17,7 +17,10 @@ struct lbm_solver {
   int host_elem = 4;  // bytes per host value (float, or double for FP64)
   void* buf[2] = {nullptr, nullptr};  // pull states; buf[cur] is the current one
   int cur = 0;
-  uint32_t t = 0;  // lattice steps taken (stochastic-rounding key of the 16-bit forms)
+  uint32_t* step_ctr = nullptr;  // device: lattice steps taken (stochastic-rounding key)
+  cudaGraphExec_t graph = nullptr;  // kGraphSteps step launches (see solver_step_raw)
+  int graph_cur = -1;               // buffer parity the graph was captured from
+  bool graphs = true;               // false after a failed capture
   size_t state_bytes = 0;
   uint32_t* mask_d = nullptr;  // bit-packed mask with periodic ghost bits
   uint32_t* body_d = nullptr;  // bit-packed body of lbm_body_force (null: every solid cell)
@@ -46,6 +49,8 @@ struct lbm_solver {
 namespace lbm_b200 {
 
 // Enqueues `steps` steps without argument checks.
+constexpr int kGraphSteps = 32;  // step launches per captured graph (even)
+void drop_step_graph(lbm_solver* s);
 int solver_step_raw(lbm_solver* s, int steps);
 // Two-pass FP64 mass reduction of the pull state `state` into *out (device), using `partials`
 // (device, `blocks` doubles) as scratch.

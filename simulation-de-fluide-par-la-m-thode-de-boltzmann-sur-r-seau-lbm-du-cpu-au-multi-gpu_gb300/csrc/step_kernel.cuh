@@ -35,9 +35,17 @@ struct StepArgs {
   typename Phys::Consts k;
   T eq_in[kQ];  // inlet equilibrium (open domain)
   PlaneScales sc;
-  uint32_t rkey;       // stochastic-rounding key of this step (16-bit forms)
-  long long key_base;  // cell offset of this grid in the rounding hash (batched instances)
+  const uint32_t* step_ctr;  // lattice steps taken before this launch sequence (device counter)
+  uint32_t step_off;         // index of this launch in the sequence
+  long long key_base;        // cell offset of this grid in the rounding hash (batched instances)
 };
+
+// Stochastic-rounding key of the step a launch performs (16-bit forms): the step index comes
+// from a device counter plus the launch's offset, so that graph replays draw fresh keys.
+template <class ST, class Phys>
+__device__ __forceinline__ uint32_t step_rkey(const StepArgs<ST, Phys>& p) {
+  return sr_step_key(__ldg(p.step_ctr) + p.step_off);
+}
 
 // Exact (bit-for-bit with v0) physics, one cell at a time (FP64).
 template <class A>
@@ -270,7 +278,7 @@ __device__ __forceinline__ void process_chunk(const StepArgs<ST, Phys>& p, const
   if (c.active) {
     using SS = StepStore<ST, G>;
     uint32_t ph[SS::kPairs];
-    SS::hashes(p.key_base + static_cast<long long>(y) * pitch + x0, p.rkey, ph);
+    if constexpr (SS::kSr) SS::hashes(p.key_base + static_cast<long long>(y) * pitch + x0, step_rkey(p), ph);
 #pragma unroll
     for (int i = 0; i < kQ; ++i)
       SS::store(p.dst + i * plane + static_cast<long long>(y) * pitch + x0, out[i], i, p.sc, ph);

@@ -220,7 +220,7 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
   }
   float2 out[kQ];
   collide_fast_t<FastF32x2>(v, p.k, out);
-  const uint32_t ph = sr_pair_hash(p.key_base + row + x, p.rkey);
+  const uint32_t ph = sr_pair_hash(p.key_base + row + x, step_rkey(p));
   uint32_t* d = reinterpret_cast<uint32_t*>(p.dst + row + x);
 #pragma unroll
   for (int i = 0; i < kQ; ++i) d[i * (plane / 2)] = encode_pair_sr<ST>(out[i].x, out[i].y, i, ph);

@@ -265,7 +265,7 @@ __device__ __forceinline__ void consume_cells(const StepArgs<ST, Phys>& p, const
   Phys::template collide_all<G>(v, p.k, out);
   using SS = StepStore<ST, G>;
   uint32_t ph[SS::kPairs];
-  SS::hashes(p.key_base + static_cast<long long>(y) * pitch + x0, p.rkey, ph);
+  if constexpr (SS::kSr) SS::hashes(p.key_base + static_cast<long long>(y) * pitch + x0, step_rkey(p), ph);
 #pragma unroll
   for (int i = 0; i < kQ; ++i)
     SS::store(p.dst + i * plane + static_cast<long long>(y) * pitch + x0, out[i], i, p.sc, ph);

@@ -86,3 +86,19 @@ def test_cylinder_velocity_error_against_fp64(gpu_lib, cylinder_ref, form):
     print(f"\ncylinder {nx}x{ny} {steps} steps {form}: {r}")
     assert r["velocity_l2"] <= VELOCITY_L2_MAX[form], r
     assert abs(r["mass_drift"]) < 1e-3, r
+
+
+@pytest.mark.parametrize("form", ["fp32", "fp16", "bf16"])
+def test_graph_replay_equals_single_launches(gpu_lib, form):
+    """Long runs replay CUDA graphs of step launches; the 16-bit forms read their rounding key
+    from a device step counter, so replays and single launches give the same bits."""
+    nx, ny = 300, 70
+    mask = gpu_lib.workloads.cylinder_wake(nx, ny, d=12.0, xc=60.0, yc=36.0)
+    with gpu_lib.Solver(nx, ny, 0.56, 2e-6, 0.0, mask, precision=form) as a, \
+            gpu_lib.Solver(nx, ny, 0.56, 2e-6, 0.0, mask, precision=form) as b:
+        a.init_equilibrium(1.0, 0.03, 0.0)
+        b.init_equilibrium(1.0, 0.03, 0.0)
+        a.run(203)  # graphs of 32 launches, then single launches
+        for _ in range(203):
+            b.step(1)
+        assert np.array_equal(a.populations(), b.populations())
