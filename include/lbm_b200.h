@@ -253,6 +253,33 @@ int lbm_batch_info(const lbm_batch* b, int* count, long long* total_cells, int* 
 /* Largest ny accepted by lbm_total_mass_noalloc (rows of its static scratch). */
 #define LBM_NOALLOC_MAX_ROWS 16384
 
+/* ------------------------------------------------------------------------------------------
+ * Strip engine: the reference's multi-rank solver (src/v4_mpi_cuda, SolverV4 over StripEngine,
+ * engine.hpp:34-62) with the ranks' strips held by one GPU. The lattice is cut into `strips`
+ * horizontal strips as the reference's make_strip does (decomposition.hpp:19-33: ny / strips
+ * rows each, the first ny % strips one more, at least 2), each with a ghost row below and
+ * above; a step runs the step kernel on every strip's owned rows, then one device launch
+ * exchanges the halos (populations 2, 5, 6 of each strip's top row into the ghost row below
+ * the strip above, 4, 7, 8 of its bottom row into the ghost row above the strip below: the
+ * reference's 3 * nx-value messages, engine.hpp:14-20), with no host staging. Results are
+ * bit-for-bit those of lbm_create / lbm_step on the whole lattice (and of the reference's v0
+ * in FP32 / FP64) for any number of strips. Host arrays as for the solver (v0 layout).
+ * ------------------------------------------------------------------------------------------ */
+typedef struct lbm_strips lbm_strips;
+int lbm_strips_create(int nx, int ny, const uint8_t* solid, double tau, double fx, double fy,
+                      int precision, int strips, lbm_strips** out);
+int lbm_strips_destroy(lbm_strips* h);
+const char* lbm_strips_last_error(const lbm_strips* h);
+/* First global row and owned rows of each strip (arrays of `strips` ints). */
+int lbm_strips_layout(const lbm_strips* h, int* first_row, int* rows);
+int lbm_strips_set_inflow_outflow(lbm_strips* h, double u_in);
+int lbm_strips_init_equilibrium(lbm_strips* h, double rho0, double ux0, double uy0);
+int lbm_strips_set_populations(lbm_strips* h, const void* s_host);
+int lbm_strips_get_populations(lbm_strips* h, void* s_host);
+int lbm_strips_macroscopic(lbm_strips* h, void* rho, void* ux, void* uy);
+int lbm_strips_step(lbm_strips* h, int steps);
+int lbm_strips_timed_run(lbm_strips* h, int steps, double* seconds);
+
 /* Total mass of a pull state held in caller memory, without allocating any device memory.
  * No counterpart in the reference: it is an extra entry point for callers that cannot let a
  * library call cudaMalloc/cudaFree, such as hosts that own all device memory through their own

@@ -70,6 +70,17 @@ def lib() -> C.CDLL:
             "lbm_set_launch": ([vp, i, i], i),
             "lbm_set_variant": ([vp, i], i),
             "lbm_set_body": ([vp, vp], i),
+            "lbm_strips_create": ([i, i, vp, d, d, d, i, i, C.POINTER(vp)], i),
+            "lbm_strips_destroy": ([vp], i),
+            "lbm_strips_last_error": ([vp], C.c_char_p),
+            "lbm_strips_layout": ([vp, vp, vp], i),
+            "lbm_strips_set_inflow_outflow": ([vp, d], i),
+            "lbm_strips_init_equilibrium": ([vp, d, d, d], i),
+            "lbm_strips_set_populations": ([vp, vp], i),
+            "lbm_strips_get_populations": ([vp, vp], i),
+            "lbm_strips_macroscopic": ([vp, vp, vp, vp], i),
+            "lbm_strips_step": ([vp, i], i),
+            "lbm_strips_timed_run": ([vp, i, C.POINTER(d)], i),
             "lbm_body_force": ([vp, C.POINTER(d), C.POINTER(d)], i),
             "lbm_state_view": ([vp, C.POINTER(vp), C.POINTER(C.c_longlong), C.POINTER(i)], i),
             "lbm_adj_create": ([i, i, vp, d, d, d, i, i, i, C.POINTER(vp)], i),
@@ -442,6 +453,83 @@ class Batch:
         n, cells, items = C.c_int(), C.c_longlong(), C.c_int()
         self._check(lib().lbm_batch_info(self._h, C.byref(n), C.byref(cells), C.byref(items)))
         return {"count": n.value, "cells": cells.value, "chunks": items.value}
+
+
+class Strips:
+    """The lattice as horizontal strips with ghost rows and a device halo exchange (C ABI
+    lbm_strips_*): the reference's multi-rank solver (src/v4_mpi_cuda) with every strip on one
+    GPU. Same results as Solver on the whole lattice, for any number of strips."""
+
+    def __init__(self, nx, ny, tau, fx, fy, solid, strips, precision="fp32"):
+        self.precision = PRECISIONS[precision] if isinstance(precision, str) else int(precision)
+        self.dtype = HOST_DTYPE[self.precision]
+        self._nx, self._ny, self.strips = int(nx), int(ny), int(strips)
+        self._solid = np.ascontiguousarray(solid, dtype=np.uint8).reshape(-1)
+        if self._solid.size != self._nx * self._ny:
+            raise ValueError("solid must hold nx*ny values")
+        self._h = C.c_void_p()
+        rc = lib().lbm_strips_create(self._nx, self._ny, _ptr(self._solid), tau, fx, fy,
+                                     self.precision, self.strips, C.byref(self._h))
+        if rc != OK:
+            _raise(rc, "lbm_strips_create failed")
+
+    def _check(self, rc):
+        if rc != OK:
+            _raise(rc, (lib().lbm_strips_last_error(self._h) or b"").decode())
+
+    def close(self):
+        if self._h:
+            lib().lbm_strips_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def layout(self):
+        y0 = np.zeros(self.strips, np.int32)
+        n = np.zeros(self.strips, np.int32)
+        self._check(lib().lbm_strips_layout(self._h, _ptr(y0), _ptr(n)))
+        return y0, n
+
+    def set_inflow_outflow(self, u_in):
+        self._check(lib().lbm_strips_set_inflow_outflow(self._h, u_in))
+
+    def init_equilibrium(self, rho0, ux0, uy0):
+        self._check(lib().lbm_strips_init_equilibrium(self._h, rho0, ux0, uy0))
+
+    def set_populations(self, s):
+        s = np.ascontiguousarray(s, dtype=self.dtype).reshape(-1)
+        if s.size != self._nx * self._ny * 9:
+            raise ValueError("populations must hold nx*ny*9 values")
+        self._check(lib().lbm_strips_set_populations(self._h, _ptr(s)))
+
+    def populations(self):
+        out = np.empty(self._nx * self._ny * 9, self.dtype)
+        self._check(lib().lbm_strips_get_populations(self._h, _ptr(out)))
+        return out
+
+    def macroscopic(self):
+        n = self._nx * self._ny
+        rho, ux, uy = (np.empty(n, self.dtype) for _ in range(3))
+        self._check(lib().lbm_strips_macroscopic(self._h, _ptr(rho), _ptr(ux), _ptr(uy)))
+        return rho, ux, uy
+
+    def run(self, steps):
+        self._check(lib().lbm_strips_step(self._h, steps))
+
+    def timed_run(self, steps) -> float:
+        t = C.c_double()
+        self._check(lib().lbm_strips_timed_run(self._h, steps, C.byref(t)))
+        return t.value
 
 
 def version() -> str:

@@ -22,66 +22,11 @@
 #include "step_async.cuh"
 #include "step_ring.cuh"
 #include "step_tma.cuh"
+#include "forms.cuh"
 
 using namespace lbm_b200;
 
 namespace {
-
-template <class ST>
-struct Form;
-template <>
-struct Form<float> {
-  using A = ExactF32;
-  using Phys = ExactPhys<ExactF32>;
-  using PackedPhys = ExactPhysF32x2;
-  static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_collide_consts<float>(float(tau), float(fx), float(fy));
-  }
-};
-template <>
-struct Form<double> {
-  using A = ExactF64;
-  using Phys = ExactPhys<ExactF64>;
-  using PackedPhys = Phys;
-  static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_collide_consts<double>(tau, fx, fy);
-  }
-};
-template <>
-struct Form<__half> {
-  using A = ExactF32;  // moment pass
-  using Phys = FastPhys;
-  using PackedPhys = Phys;  // already packed
-  static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_fast_consts(float(tau), float(fx), float(fy), kStoreScale16);
-  }
-};
-template <>
-struct Form<__nv_bfloat16> {
-  using A = ExactF32;
-  using Phys = FastPhys;
-  using PackedPhys = Phys;  // already packed
-  static Phys::Consts consts(double tau, double fx, double fy) {
-    return make_fast_consts(float(tau), float(fx), float(fy), kStoreScale16);
-  }
-};
-
-constexpr int kCx[kQ] = {0, 1, 0, -1, 0, 1, -1, -1, 1};
-constexpr int kCy[kQ] = {0, 0, 1, 0, -1, 1, 1, -1, -1};
-
-// Shifted equilibrium of (rho0, ux0, uy0) in T, the reference's expressions and order
-// (src/common/boundary.hpp:26-34, src/common/d2q9.hpp:40-42).
-template <class T>
-Eq9<T> host_equilibrium(T rho0, T ux0, T uy0) {
-  Eq9<T> e{};
-  const T usq = ux0 * ux0 + uy0 * uy0;
-  const T drho0 = rho0 - T(1);
-  for (int i = 0; i < kQ; ++i) {
-    const T cu = kCx[i] * ux0 + kCy[i] * uy0;
-    e.v[i] = weight<T>(i) * (drho0 + rho0 * (T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq));
-  }
-  return e;
-}
 
 int set_error(lbm_solver* s, int code, const std::string& msg) {
   if (s) s->err = msg;
@@ -274,15 +219,13 @@ int launch_ring_t(lbm_solver* s, int steps) {
       a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
       a.step_ctr = s->step_ctr;
       a.step_off = static_cast<uint32_t>(k);
-      kernel<<<grid, S::kThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
+      kernel<<<grid, S::kThreads, smem, s->stream>>>(a, tpr, tiles, 0, s->err_flag);
       s->cur ^= 1;
     }
     LBM_CUDA(s, cudaGetLastError());
     return LBM_OK;
   }
 }
-
-constexpr int kMaskPadWords = 80;
 
 // Automatic kernel choice (variant < 0): the ring kernel when there are at least two of its
 // tiles per SM (plain FP32 / FP64: 12, 63 registers, 3 resident blocks; 16-bit storage: 17, the
@@ -585,14 +528,10 @@ int lbm_create(int nx, int ny, const uint8_t* solid, double tau, double fx, doub
 
   const int per_line = 128 / elem;
   const int pitch = (nx + per_line - 1) / per_line * per_line;
-  // Mask rows extend kMaskPadWords words (all solid) past the row: a staged copy of a tile's
-  // mask words reads up to the tile width / 32 + 4 words (at most 68) from the tile's first word,
-  // and lanes past the row end read their (all-solid) window. The word count is a multiple of 4
-  // so that every row starts on a 16-byte boundary (asynchronous-copy alignment).
   s->g.nx = nx;
   s->g.ny = ny;
   s->g.pitch = pitch;
-  s->g.mask_words = ((nx + 31) / 32 + kMaskPadWords + 3) / 4 * 4;
+  s->g.mask_words = mask_row_words(nx);
   s->g.plane = static_cast<long long>(pitch) * ny;
   s->g.open_x = 0;
 

@@ -48,9 +48,9 @@ struct lbm_solver {
 
 namespace lbm_b200 {
 
-// Enqueues `steps` steps without argument checks.
 constexpr int kGraphSteps = 32;  // step launches per captured graph (even)
 void drop_step_graph(lbm_solver* s);
+// Enqueues `steps` steps without argument checks (graph replays plus single launches).
 int solver_step_raw(lbm_solver* s, int steps);
 // Two-pass FP64 mass reduction of the pull state `state` into *out (device), using `partials`
 // (device, `blocks` doubles) as scratch.
@@ -58,5 +58,11 @@ int solver_mass_into(lbm_solver* s, const void* state, double* partials, int blo
 // Bit-packed mask rows with the periodic ghost bits (see lbm_device.cuh).
 void pack_mask(const uint8_t* solid, int nx, int ny, int mask_words, std::vector<uint32_t>& out);
 int element_bytes(int precision);
+// Words per bit-packed mask row: the row's bits, the ghost bits, and kMaskPadWords words (all
+// solid) past the row, so that a staged copy of a tile's mask words (at most tile width / 32 + 4
+// words from the tile's first word, 68 for the widest tile) stays inside; a multiple of 4 so
+// that every row starts on a 16-byte boundary (asynchronous-copy alignment).
+constexpr int kMaskPadWords = 80;
+inline int mask_row_words(int nx) { return ((nx + 31) / 32 + kMaskPadWords + 3) / 4 * 4; }
 
 }  // namespace lbm_b200

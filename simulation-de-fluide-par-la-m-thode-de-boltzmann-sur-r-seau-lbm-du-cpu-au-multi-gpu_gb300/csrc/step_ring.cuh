@@ -20,7 +20,9 @@
 //   * one vote per strip tells whether any of its cells or their neighbours is solid; only then
 //     are per-cell neighbour bits formed and bounce-back values read (opposite population of the
 //     cell itself, from global memory);
-//   * waits are bounded as in the bulk-copy kernel (error flag, LBM_ERR_TIMEOUT on the host).
+//   * waits are bounded as in the bulk-copy kernel (error flag, LBM_ERR_TIMEOUT on the host);
+//   * tiles cover rows row0 .. row0 + tiles / tiles_per_row - 1 (the strip engine steps the owned
+//     rows of a strip between its two ghost rows).
 #pragma once
 
 #include "step_tma.cuh"
@@ -228,7 +230,7 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
 
 template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
-    ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
+    ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int row0, int* err) {
   using S = RingShape<ST, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);
@@ -255,8 +257,9 @@ __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
         ok = false;
         break;
       }
-      const int y = tile / tiles_per_row;
-      const int tx0 = (tile - y * tiles_per_row) * S::TW;
+      const int tr = tile / tiles_per_row;
+      const int y = row0 + tr;
+      const int tx0 = (tile - tr * tiles_per_row) * S::TW;
       const int ym = y == 0 ? ny - 1 : y - 1;
       const int yp = y == ny - 1 ? 0 : y + 1;
       const int xs = tx0 - S::H > 0 ? tx0 - S::H : 0;
@@ -318,8 +321,9 @@ __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
   uint32_t phase = 0;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     if (!mbar_wait_bounded_warp(&full[s], phase, err)) return;
-    const int y = tile / tiles_per_row;
-    const int tx0 = (tile - y * tiles_per_row) * S::TW;
+    const int tr = tile / tiles_per_row;
+    const int y = row0 + tr;
+    const int tx0 = (tile - tr * tiles_per_row) * S::TW;
     const int xw = tx0 + cw * S::SW;
     if (xw < nx) {
       const unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
