@@ -241,9 +241,17 @@ int lbm_batch_run(lbm_batch* b, int steps);
 int lbm_batch_timed_run(lbm_batch* b, int steps, double* seconds);
 /* The comparison point: the same steps with one launch per instance per step. */
 int lbm_batch_run_separate(lbm_batch* b, int steps, double* seconds);
-/* Launch shape: cells per thread (the two vector widths of the form, 0 = widest), threads per
- * block (multiple of 32, <= 256), blocks (0 = all resident blocks). */
+/* Launch shape. cells_per_thread 0 or 1: the warp-specialised ring kernel (one cell, or one
+ * pair with 16-bit storage, per lane; the default) with the tile shape of lbm_batch_set_tiles;
+ * the form's two vector widths (FP32: 4, 2; FP64: 2; 16-bit: 8, 4): the chunk kernel with that
+ * many cells per thread and block_threads threads per block (multiple of 32, <= 256).
+ * grid_blocks: blocks (0 = all resident blocks). */
 int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, int grid_blocks);
+/* Tile shape of the ring kernel (selects it): consumer warps x passes per tile, one of 8x2
+ * (the default), 4x2, 4x1, 2x2, and the ring depth (2 or 4 stages); a tile spans
+ * warps * passes * 32 cells of a row (twice that with 16-bit storage), so narrow instances waste
+ * fewer lanes with smaller shapes, and deeper rings keep more bytes in flight per block. */
+int lbm_batch_set_tiles(lbm_batch* b, int consumer_warps, int passes, int stages);
 /* Times the candidate launch shapes on the current ensemble and keeps the fastest; with a cache
  * path the choice is read from / appended to that file (one line per GPU, form and size). The
  * state is restored afterwards. report (may be null) receives a one-line summary. */

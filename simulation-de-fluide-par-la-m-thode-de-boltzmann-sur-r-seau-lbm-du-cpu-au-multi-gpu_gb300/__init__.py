@@ -103,6 +103,7 @@ def lib() -> C.CDLL:
             "lbm_batch_timed_run": ([vp, i, C.POINTER(d)], i),
             "lbm_batch_run_separate": ([vp, i, C.POINTER(d)], i),
             "lbm_batch_set_launch": ([vp, i, i, i], i),
+            "lbm_batch_set_tiles": ([vp, i, i, i], i),
             "lbm_batch_autotune": ([vp, C.c_char_p, C.c_char_p, C.c_size_t], i),
             "lbm_batch_info": ([vp, C.POINTER(i), C.POINTER(C.c_longlong), C.POINTER(i)], i),
         }
@@ -442,6 +443,11 @@ class Batch:
 
     def set_launch(self, cells_per_thread=0, block_threads=256, grid_blocks=0):
         self._check(lib().lbm_batch_set_launch(self._h, cells_per_thread, block_threads, grid_blocks))
+
+    def set_tiles(self, consumer_warps=8, passes=2, stages=2):
+        """Ring-kernel tile shape (and selects the ring kernel): 8x2, 4x2, 4x1 or 2x2 with 2 or
+        4 ring stages."""
+        self._check(lib().lbm_batch_set_tiles(self._h, consumer_warps, passes, stages))
 
     def autotune(self, cache_path=None) -> str:
         buf = C.create_string_buffer(4096)

@@ -5,8 +5,10 @@
 // (offsets, geometry, collision constants, first global chunk index). The step kernel's warps
 // walk the global chunk list (chunks of 32 * G cells of one row of one instance), find their
 // instance by binary search over the first-chunk indices staged in shared memory, and run the
-// same chunk code as the single-grid kernel (step_kernel.cuh). Steps are replayed from a CUDA
-// graph of kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
+// same chunk code as the single-grid kernel (step_kernel.cuh). The default kernel is instead the
+// warp-specialised ring of the single-grid solver (step_ring.cuh) over the ensemble's tiles: a
+// tile's instance comes from a binary search over the per-instance first-tile indices staged in
+// shared memory. Steps are replayed from a CUDA graph of kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
 // instance per step (the comparison point). lbm_batch_autotune() times the candidate launch
 // shapes (cells per thread G, i.e. the chunk width 32 G, threads per block, blocks per SM) on the
 // actual ensemble and keeps the fastest, caching the choice per GPU, form and ensemble size.
@@ -25,7 +27,9 @@
 #include "aux_kernels.cuh"
 #include "lbm_b200.h"
 #include "solver_internal.h"
+#include "forms.cuh"
 #include "step_kernel.cuh"
+#include "step_ring.cuh"
 
 using namespace lbm_b200;
 
@@ -42,6 +46,8 @@ struct BatchInst {
   Grid2D g;
   int cpr;     // chunks per row for the launch's G
   int item0;   // first global chunk index
+  int tpr;     // ring tiles per row
+  int tile0;   // first global ring tile index
   Consts k;
 };
 
@@ -100,6 +106,58 @@ __global__ void __launch_bounds__(kBatchThreads)
   }
 }
 
+// Tiles of the ensemble for the ring pipeline: instance by binary search over the first-tile
+// indices in shared memory, then that instance's grid from the table.
+template <class ST, class Phys, int kTW>
+struct BatchTiles {
+  const BatchArgs<ST, Phys>& a;
+  const int* s_tile0;
+  template <class F>
+  __device__ __forceinline__ void visit(int tile, F&& f) const {
+    int lo = 0, hi = a.count - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (s_tile0[mid] <= tile)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const BatchInst<typename Phys::Consts>& d = a.inst[lo];
+    StepArgs<ST, Phys> p;
+    p.src = a.src + d.off;
+    p.dst = a.dst + d.off;
+    p.mask = a.mask + d.mask_off;
+    p.g = d.g;
+    p.k = d.k;
+    p.sc = a.sc;
+    p.step_ctr = a.step;
+    p.step_off = 0;
+    p.key_base = d.off / kQ;
+    const int local = tile - s_tile0[lo];
+    const int tr = local / d.tpr;
+    f(p, tr, (local - tr * d.tpr) * kTW);
+  }
+};
+
+// Resident blocks per SM the register budget of a ring shape is capped for: 27 to 30 warps per SM
+// for the FP32 and 16-bit collisions (72 to 80 registers), none for FP64 (FP64-ALU-bound).
+template <class ST, int kW>
+constexpr int batch_ring_min_blocks() {
+  return sizeof(ST) == 8 ? 1 : (kW == 8 ? 3 : (kW == 4 ? 5 : 8));
+}
+
+template <class ST, class Phys, int kW, int kC, int kStages>
+__global__ void __launch_bounds__(32 * (kW + 1), (batch_ring_min_blocks<ST, kW>()))
+    batch_ring_kernel(const BatchArgs<ST, Phys> a, int tiles, int* err) {
+  using S = RingShape<ST, kW, kC>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  int* s_tile0 = reinterpret_cast<int*>(smem + ring_smem_bytes<S>(kStages));
+  for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_tile0[k] = a.inst[k].tile0;
+  __syncthreads();
+  const BatchTiles<ST, Phys, S::TW> tiles_of{a, s_tile0};
+  ring_pipeline<ST, Phys, false, kW, kC, kStages>(smem, tiles_of, tiles, err);
+}
+
 template <class ST>
 struct BForm;
 template <>
@@ -154,13 +212,17 @@ struct lbm_batch {
   int red_blocks = 0;
   PlaneScales sc{};
   // launch configuration (autotuned)
-  int G = 0, block = kBatchThreads, grid = 0, items = 0, grid_eff = 1;
+  // G: cells per thread of the chunk kernel (V or V / 2), or 1 (also 0, the default) for the
+  // ring kernel; tiles: the ring kernel's tile count
+  int G = 0, block = kBatchThreads, grid = 0, items = 0, tiles = 0, grid_eff = 1;
+  int ring_w = 8, ring_c = 2, ring_s = 2;  // ring tile shape: consumer warps, passes; stages
+  int table_tw = 0;            // ring tile width the table's tile indices were built for
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaGraphExec_t graph = nullptr;
   int graph_cur = -1;  // buffer parity the graph was captured from
   uint32_t t = 0;             // lattice steps taken (host copy of *step_d)
-  uint32_t* step_d = nullptr;  // device step counter
+  uint32_t* step_d = nullptr;  // device: [0] step counter, [1] error flag of the bounded waits
   int sm_count = 0, device = 0;
   std::string err, tune_report;
 };
@@ -193,7 +255,7 @@ template <class ST>
 int build_table(lbm_batch* b, int G) {
   using Consts = typename BForm<ST>::Phys::Consts;
   std::vector<BatchInst<Consts>> tab(b->count);
-  int item = 0;
+  int item = 0, tile = 0;
   for (int k = 0; k < b->count; ++k) {
     const auto& in = b->inst[k];
     BatchInst<Consts>& d = tab[k];
@@ -202,9 +264,13 @@ int build_table(lbm_batch* b, int G) {
     d.g = in.g;
     d.cpr = (in.nx + 32 * G - 1) / (32 * G);
     d.item0 = item;
+    d.tpr = (in.nx + b->table_tw - 1) / b->table_tw;
+    d.tile0 = tile;
     d.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
     item += d.cpr * in.ny;
+    tile += d.tpr * in.ny;
   }
+  b->tiles = tile;
   if (!b->table_d) B_CUDA(b, cudaMalloc(&b->table_d, b->count * sizeof(BatchInst<Consts>)));
   B_CUDA(b, cudaMemcpy(b->table_d, tab.data(), b->count * sizeof(BatchInst<Consts>), cudaMemcpyHostToDevice));
   b->items = item;
@@ -218,8 +284,10 @@ int launch_batch_t(lbm_batch* b, int steps, bool prepare_only) {
   const auto kernel = batch_step_kernel<ST, Phys, G>;
   if (prepare_only) {
     // Everything that is not a stream operation happens here, outside any graph capture.
-    if (b->table_G != G)
+    if (b->table_G != G) {
+      if (b->table_tw == 0) b->table_tw = RingShape<ST, 8, 2>::TW;
       if (int rc = build_table<ST>(b, G)) return rc;
+    }
     int grid = b->grid;
     if (grid <= 0) {
       int per_sm = 0;
@@ -249,12 +317,68 @@ int launch_batch_t(lbm_batch* b, int steps, bool prepare_only) {
   return LBM_OK;
 }
 
+// The ring kernel over the ensemble's tiles (one cell, or a pair with 16-bit storage, per lane),
+// tile shape kW consumer warps x kC passes, kStages ring stages per block.
+template <class ST, int kW, int kC, int kStages>
+int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
+  using Phys = typename BForm<ST>::Phys;
+  using S = RingShape<ST, kW, kC>;
+  const auto kernel = batch_ring_kernel<ST, Phys, kW, kC, kStages>;
+  const size_t smem = ring_smem_bytes<S>(kStages) + static_cast<size_t>(b->count) * sizeof(int);
+  if (prepare_only) {
+    if (b->table_G == 0 || b->table_tw != S::TW) {
+      b->table_tw = S::TW;
+      if (int rc = build_table<ST>(b, b->table_G ? b->table_G : StoreTraits<ST>::kVec)) return rc;
+    }
+    B_CUDA(b, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
+    int grid = b->grid;
+    if (grid <= 0) {
+      int per_sm = 0;
+      B_CUDA(b, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, S::kThreads, smem));
+      grid = std::max(1, per_sm) * b->sm_count;
+    }
+    b->grid_eff = std::max(1, std::min(grid, b->tiles));
+    return LBM_OK;
+  }
+  BatchArgs<ST, Phys> a{};
+  a.mask = b->mask_d;
+  a.inst = static_cast<const BatchInst<typename Phys::Consts>*>(b->table_d);
+  a.count = b->count;
+  a.items = b->items;
+  a.sc = b->sc;
+  a.step = b->step_d;
+  int* err = reinterpret_cast<int*>(b->step_d + 1);
+  for (int s = 0; s < steps; ++s) {
+    a.src = static_cast<const ST*>(b->buf[b->cur]);
+    a.dst = static_cast<ST*>(b->buf[b->cur ^ 1]);
+    kernel<<<b->grid_eff, S::kThreads, smem, b->stream>>>(a, b->tiles, err);
+    step_counter_add<<<1, 1, 0, b->stream>>>(b->step_d);
+    ++b->t;
+    b->cur ^= 1;
+  }
+  const cudaError_t e = cudaPeekAtLastError();
+  if (e != cudaSuccess) return bfail(b, LBM_ERR_CUDA, std::string("batch launch: ") + cudaGetErrorString(e));
+  return LBM_OK;
+}
+
+template <class ST>
+int launch_batch_ring(lbm_batch* b, int steps, bool prepare_only) {
+  const bool deep = b->ring_s == 4;
+  if (b->ring_w == 4 && b->ring_c == 2)
+    return deep ? launch_batch_ring_t<ST, 4, 2, 4>(b, steps, prepare_only) : launch_batch_ring_t<ST, 4, 2, 2>(b, steps, prepare_only);
+  if (b->ring_w == 4 && b->ring_c == 1)
+    return deep ? launch_batch_ring_t<ST, 4, 1, 4>(b, steps, prepare_only) : launch_batch_ring_t<ST, 4, 1, 2>(b, steps, prepare_only);
+  if (b->ring_w == 2 && b->ring_c == 2)
+    return deep ? launch_batch_ring_t<ST, 2, 2, 4>(b, steps, prepare_only) : launch_batch_ring_t<ST, 2, 2, 2>(b, steps, prepare_only);
+  return deep ? launch_batch_ring_t<ST, 8, 2, 4>(b, steps, prepare_only) : launch_batch_ring_t<ST, 8, 2, 2>(b, steps, prepare_only);
+}
+
 template <class ST>
 int launch_batch(lbm_batch* b, int steps, bool prepare_only) {
   constexpr int V = StoreTraits<ST>::kVec;
   constexpr int H = V / 2 >= 2 ? V / 2 : V;  // the narrower vector (8 bytes), FP64 keeps 16
-  const int G = b->G > 0 ? b->G : V;
-  if (G == H && H != V) return launch_batch_t<ST, H>(b, steps, prepare_only);
+  if (b->G <= 1) return launch_batch_ring<ST>(b, steps, prepare_only);
+  if (b->G == H && H != V) return launch_batch_t<ST, H>(b, steps, prepare_only);
   return launch_batch_t<ST, V>(b, steps, prepare_only);
 }
 
@@ -443,6 +567,18 @@ int get_pop_t(lbm_batch* b, int k, void* host) {
   return LBM_OK;
 }
 
+// Reads and clears the error flag of the ring kernel's bounded waits (after a synchronisation).
+int check_batch_flag(lbm_batch* b) {
+  uint32_t flag = 0;
+  B_CUDA(b, cudaMemcpyAsync(&flag, b->step_d + 1, sizeof(flag), cudaMemcpyDeviceToHost, b->stream));
+  B_CUDA(b, cudaStreamSynchronize(b->stream));
+  if (flag) {
+    B_CUDA(b, cudaMemsetAsync(b->step_d + 1, 0, sizeof(flag), b->stream));
+    return bfail(b, LBM_ERR_TIMEOUT, "a step kernel gave up waiting for its shared-memory ring");
+  }
+  return LBM_OK;
+}
+
 int time_steps(lbm_batch* b, int steps, double* seconds) {
   B_CUDA(b, cudaEventRecord(b->ev[0], b->stream));
   if (int rc = batch_run(b, steps)) return rc;
@@ -451,7 +587,7 @@ int time_steps(lbm_batch* b, int steps, double* seconds) {
   float ms = 0.f;
   B_CUDA(b, cudaEventElapsedTime(&ms, b->ev[0], b->ev[1]));
   *seconds = ms * 1e-3;
-  return LBM_OK;
+  return check_batch_flag(b);
 }
 
 std::string tune_key(const lbm_batch* b) {
@@ -509,8 +645,7 @@ int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* con
     in.g.nx = nx[k];
     in.g.ny = ny[k];
     in.g.pitch = (nx[k] + per_line - 1) / per_line * per_line;
-    const int span = 32 * b->vec;
-    in.g.mask_words = (nx[k] + span - 1) / span * b->vec + 2;
+    in.g.mask_words = mask_row_words(nx[k]);
     in.g.plane = static_cast<long long>(in.g.pitch) * ny[k];
     in.g.open_x = 0;
     in.off = off;
@@ -541,8 +676,8 @@ int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* con
     e = cudaMemcpy(b->mask_d, all_words.data(), all_words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
   b->red_blocks = 4 * b->sm_count;
   if (e == cudaSuccess) e = cudaMalloc(&b->red, (b->red_blocks + 2) * sizeof(double));
-  if (e == cudaSuccess) e = cudaMalloc(&b->step_d, sizeof(uint32_t));
-  if (e == cudaSuccess) e = cudaMemset(b->step_d, 0, sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMalloc(&b->step_d, 4 * sizeof(uint32_t));
+  if (e == cudaSuccess) e = cudaMemset(b->step_d, 0, 4 * sizeof(uint32_t));
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
   *out = b;
   return LBM_OK;
@@ -601,8 +736,7 @@ int lbm_batch_total_mass(lbm_batch* b, int instance, double* mass) {
 int lbm_batch_run(lbm_batch* b, int steps) {
   if (!b || steps < 0) return bfail(b, LBM_ERR_INVALID_ARG, "steps must be >= 0");
   if (int rc = batch_run(b, steps)) return rc;
-  B_CUDA(b, cudaStreamSynchronize(b->stream));
-  return LBM_OK;
+  return check_batch_flag(b);
 }
 
 int lbm_batch_timed_run(lbm_batch* b, int steps, double* seconds) {
@@ -633,7 +767,7 @@ int lbm_batch_run_separate(lbm_batch* b, int steps, double* seconds) {
 int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, int grid_blocks) {
   if (!b) return LBM_ERR_INVALID_ARG;
   const int V = b->vec, H = V / 2 >= 2 ? V / 2 : V;
-  if ((cells_per_thread != 0 && cells_per_thread != V && cells_per_thread != H) ||
+  if ((cells_per_thread > 1 && cells_per_thread != V && cells_per_thread != H) || cells_per_thread < 0 ||
       block_threads % 32 != 0 || block_threads <= 0 || block_threads > kBatchThreads || grid_blocks < 0)
     return bfail(b, LBM_ERR_INVALID_ARG, "bad launch configuration");
   b->G = cells_per_thread;
@@ -643,21 +777,54 @@ int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, 
   return LBM_OK;
 }
 
+int lbm_batch_set_tiles(lbm_batch* b, int consumer_warps, int passes, int stages) {
+  if (!b) return LBM_ERR_INVALID_ARG;
+  const bool ok = ((consumer_warps == 8 && passes == 2) || (consumer_warps == 4 && passes == 2) ||
+                   (consumer_warps == 4 && passes == 1) || (consumer_warps == 2 && passes == 2)) &&
+                  (stages == 2 || stages == 4);
+  if (!ok) return bfail(b, LBM_ERR_INVALID_ARG, "tile shape must be 8x2, 4x2, 4x1 or 2x2, with 2 or 4 stages");
+  b->ring_w = consumer_warps;
+  b->ring_c = passes;
+  b->ring_s = stages;
+  b->G = 0;
+  drop_graph(b);
+  return LBM_OK;
+}
+
 int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_t report_size) {
   if (!b) return LBM_ERR_INVALID_ARG;
   const std::string key = tune_key(b);
-  // Cached choice?
+  struct Cand {
+    int G, blk, per_sm, w, c, s;  // G <= 1: ring kernel of tile shape w x c, s stages
+    double t;
+  };
+  auto apply = [&](const Cand& c) {
+    if (c.G <= 1)
+      if (int rc = lbm_batch_set_tiles(b, c.w, c.c, c.s)) return rc;
+    return lbm_batch_set_launch(b, c.G, c.blk, c.per_sm * b->sm_count);
+  };
+  auto describe = [&](const Cand& c) {
+    std::ostringstream d;
+    if (c.G <= 1)
+      d << "ring " << c.w << "x" << c.c << " stages=" << c.s << " grid=" << c.per_sm * b->sm_count;
+    else
+      d << "G=" << c.G << " block=" << c.blk << " grid=" << c.per_sm * b->sm_count;
+    return d.str();
+  };
+  // Cached choice? Lines: key \t G block grid [warps passes].
   if (cache_path) {
     std::ifstream in(cache_path);
     std::string line;
     while (std::getline(in, line)) {
       std::istringstream ls(line);
       std::string k;
-      int G, blk, grd;
+      int G, blk, grd, w = 8, c = 2, s = 2;
       if (std::getline(ls, k, '\t') && k == key && (ls >> G >> blk >> grd)) {
-        if (lbm_batch_set_launch(b, G, blk, grd) == LBM_OK) {
-          b->tune_report = "cached: G=" + std::to_string(G) + " block=" + std::to_string(blk) +
-                           " grid=" + std::to_string(grd);
+        ls >> w >> c >> s;
+        const Cand cand{G, blk, grd / std::max(1, b->sm_count), w, c, s, 0.0};
+        if (apply(cand) == LBM_OK) {
+          b->grid = grd;
+          b->tune_report = "cached: " + describe(cand);
           if (report && report_size) std::snprintf(report, report_size, "%s", b->tune_report.c_str());
           return LBM_OK;
         }
@@ -672,21 +839,26 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
   B_CUDA(b, cudaMalloc(&saved, bytes));
   B_CUDA(b, cudaMemcpyAsync(saved, b->buf[b->cur], bytes, cudaMemcpyDeviceToDevice, b->stream));
   const int V = b->vec, H = V / 2 >= 2 ? V / 2 : V;
-  struct Cand {
-    int G, blk, per_sm;
-    double t;
-  };
   std::vector<Cand> cands;
-  for (int G : {V, H}) {
-    if (G == H && H == V && !cands.empty() && cands.back().G == G) continue;
+  // Ring kernel: tile shape x stages x resident blocks per SM (up to what the register and
+  // shared-memory budgets let reside).
+  const int shapes[6][3] = {{8, 2, 2}, {4, 2, 2}, {4, 2, 4}, {4, 1, 4}, {2, 2, 2}, {2, 2, 4}};
+  for (const auto& sh : shapes)
+    for (int per_sm : {1, 2, 3, 4, 5, 6, 8})
+      if (per_sm <= (sh[0] == 8 ? 3 : (sh[0] == 4 ? 5 : 8))) cands.push_back({1, kBatchThreads, per_sm, sh[0], sh[1], sh[2], 0.0});
+  for (int G : {V, H}) {  // chunk kernel: cells per thread x block x blocks per SM
+    if (G == H && H == V) continue;
     for (int blk : {128, 256})
-      for (int per_sm : {1, 2, 4, 8}) cands.push_back({G, blk, per_sm, 0.0});
+      for (int per_sm : {1, 2, 4, 8}) cands.push_back({G, blk, per_sm, 8, 2, 2, 0.0});
   }
+  if (H == V)
+    for (int blk : {128, 256})
+      for (int per_sm : {1, 2, 4, 8}) cands.push_back({V, blk, per_sm, 8, 2, 2, 0.0});
   double best = 1e30;
   Cand pick = cands.front();
   std::ostringstream rep;
   for (Cand& c : cands) {
-    if (int rc = lbm_batch_set_launch(b, c.G, c.blk, c.per_sm * b->sm_count)) {
+    if (int rc = apply(c)) {
       cudaFree(saved);
       return rc;
     }
@@ -700,8 +872,9 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
       return rc;
     }
     c.t = t;
-    rep << "G" << c.G << "/b" << c.blk << "/x" << c.per_sm << ":" << static_cast<long long>(b->total_cells * 16 / t / 1e6)
-        << " ";
+    rep << (c.G <= 1 ? "R" + std::to_string(c.w) + "x" + std::to_string(c.c) + "s" + std::to_string(c.s)
+                     : "G" + std::to_string(c.G) + "/b" + std::to_string(c.blk))
+        << "/x" << c.per_sm << ":" << static_cast<long long>(b->total_cells * 16 / t / 1e6) << " ";
     if (t < best) {
       best = t;
       pick = c;
@@ -712,12 +885,12 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
   b->t = t_saved;
   B_CUDA(b, cudaStreamSynchronize(b->stream));
   cudaFree(saved);
-  if (int rc = lbm_batch_set_launch(b, pick.G, pick.blk, pick.per_sm * b->sm_count)) return rc;
-  b->tune_report = "tuned: G=" + std::to_string(pick.G) + " block=" + std::to_string(pick.blk) +
-                   " grid=" + std::to_string(pick.per_sm * b->sm_count) + " | " + rep.str();
+  if (int rc = apply(pick)) return rc;
+  b->tune_report = "tuned: " + describe(pick) + " | " + rep.str();
   if (cache_path) {
     std::ofstream outf(cache_path, std::ios::app);
-    outf << key << '\t' << pick.G << ' ' << pick.blk << ' ' << pick.per_sm * b->sm_count << '\n';
+    outf << key << '\t' << pick.G << ' ' << pick.blk << ' ' << pick.per_sm * b->sm_count << ' ' << pick.w << ' '
+         << pick.c << ' ' << pick.s << '\n';
   }
   if (report && report_size) std::snprintf(report, report_size, "%s", b->tune_report.c_str());
   return LBM_OK;

@@ -48,7 +48,7 @@ struct RingShape {
 };
 
 template <class S>
-constexpr size_t ring_smem_bytes(int stages) {
+__host__ __device__ constexpr size_t ring_smem_bytes(int stages) {
   return static_cast<size_t>(stages) * S::kStageBytes + 2 * stages * sizeof(uint64_t);
 }
 
@@ -228,15 +228,90 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
   for (int i = 0; i < kQ; ++i) d[i * (plane / 2)] = encode_pair_sr<ST>(out[i].x, out[i].y, i, ph);
 }
 
-template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
-__global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
-    ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int row0, int* err) {
+// Producer work of one tile (row y, first cell tx0) of grid p into the stage at `base`: arms the
+// stage's full barrier with the byte count, then issues the bulk copies of the 9 plane rows, the
+// 3 mask rows and, on a periodic row's first / last tile, the wrap blocks.
+template <class ST, class Phys, bool kOpen, class S>
+__device__ __forceinline__ void ring_issue_tile(const StepArgs<ST, Phys>& p, unsigned char* base,
+                                                uint64_t* full, int y, int tx0) {
+  const int nx = p.g.nx, ny = p.g.ny;
+  const int ym = y == 0 ? ny - 1 : y - 1;
+  const int yp = y == ny - 1 ? 0 : y + 1;
+  const int xs = tx0 - S::H > 0 ? tx0 - S::H : 0;
+  const int xe = tx0 + S::TW + S::H < p.g.pitch ? tx0 + S::TW + S::H : p.g.pitch;
+  const uint32_t bytes = static_cast<uint32_t>((xe - xs) * sizeof(ST));
+  const bool wrap_lo = !kOpen && tx0 == 0;
+  const bool wrap_hi = !kOpen && tx0 + S::TW >= nx;
+  mbar_arrive_expect_tx(full, kQ * bytes + S::kMaskBytes + (wrap_lo ? 48u : 0u) + (wrap_hi ? 48u : 0u));
+  ST* stage = reinterpret_cast<ST*>(base);
+#pragma unroll
+  for (int i = 0; i < kQ; ++i) {
+    const ST* src = p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xs;
+    bulk_copy_g2s(stage + i * S::SROW + (xs - (tx0 - S::H)), src, bytes, full);
+  }
+  uint32_t* smask = reinterpret_cast<uint32_t*>(base + S::kPlaneBytes);
+  const int r3[3] = {ym, y, yp};
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    bulk_copy_g2s(smask + r * S::MW, p.mask + static_cast<size_t>(r3[r]) * p.g.mask_words + (tx0 >> 5),
+                  S::MW * 4, full);
+  ST* wr = reinterpret_cast<ST*>(base + S::kPlaneBytes + S::kMaskBytes);
+  if (wrap_lo) {
+    const int xb = (nx - 1) & ~(S::H - 1);
+    for (int j = 0; j < 3; ++j) {
+      const int i = wrap_dir(j);
+      bulk_copy_g2s(wr + j * S::H,
+                    p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xb, 16, full);
+    }
+  }
+  if (wrap_hi) {
+    for (int j = 3; j < 6; ++j) {
+      const int i = wrap_dir(j);
+      bulk_copy_g2s(wr + j * S::H, p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch,
+                    16, full);
+    }
+  }
+}
+
+// Consumer work of one tile: warp cw's strip of the stage at `base`.
+template <class ST, class Phys, bool kOpen, class S, int kC>
+__device__ __forceinline__ void ring_consume_tile(const StepArgs<ST, Phys>& p, const unsigned char* base,
+                                                  int y, int tx0, int cw, int lane) {
+  const int nx = p.g.nx, ny = p.g.ny;
+  const int xw = tx0 + cw * S::SW;
+  if (xw >= nx) return;
+  const ST* st = reinterpret_cast<const ST*>(base);
+  const uint32_t* sm = reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes);
+  const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes);
+  const int ym = y == 0 ? ny - 1 : y - 1;
+  const int yp = y == ny - 1 ? 0 : y + 1;
+  const int w0 = cw * S::WPS;  // first staged mask word of the strip
+  // Any solid among the strip's cells and their neighbours (words w0 .. w0 + WPS of 3 rows).
+  uint32_t mine = 0;
+  if (lane < 3 * (S::WPS + 1)) mine = sm[(lane / (S::WPS + 1)) * S::MW + w0 + lane % (S::WPS + 1)];
+  const bool solids = __any_sync(0xffffffffu, mine != 0u);
+#pragma unroll 1
+  for (int c = 0; c < kC; ++c) {
+    const int x = xw + 32 * S::LC * c + S::LC * lane;
+    if (x < nx) {
+      if constexpr (S::LC == 2)
+        ring_pair<ST, kOpen, S>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids);
+      else
+        ring_cell<ST, typename Phys::Arith, kOpen, S>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H, w0 + c,
+                                                     lane, solids);
+    }
+  }
+}
+
+// The warp-specialised pipeline over tiles 0 .. tiles - 1, grid-stride: `tiles_of.visit(tile, f)`
+// calls f(p, y, tx0) with the grid, row and first cell of a tile (one grid for the solver, the
+// tile's instance for the batched ensemble).
+template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, class Tiles>
+__device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& tiles_of, int tiles, int* err) {
   using S = RingShape<ST, kW, kC>;
-  extern __shared__ __align__(128) unsigned char smem[];
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);
   uint64_t* empty = full + kStages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nx = p.g.nx, ny = p.g.ny;
   if (threadIdx.x == 0) {
     for (int s = 0; s < kStages; ++s) {
       mbar_init(&full[s], 1);
@@ -257,49 +332,10 @@ __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
         ok = false;
         break;
       }
-      const int tr = tile / tiles_per_row;
-      const int y = row0 + tr;
-      const int tx0 = (tile - tr * tiles_per_row) * S::TW;
-      const int ym = y == 0 ? ny - 1 : y - 1;
-      const int yp = y == ny - 1 ? 0 : y + 1;
-      const int xs = tx0 - S::H > 0 ? tx0 - S::H : 0;
-      const int xe = tx0 + S::TW + S::H < p.g.pitch ? tx0 + S::TW + S::H : p.g.pitch;
-      const uint32_t bytes = static_cast<uint32_t>((xe - xs) * sizeof(ST));
-      const bool wrap_lo = !kOpen && tx0 == 0;
-      const bool wrap_hi = !kOpen && tx0 + S::TW >= nx;
-      mbar_arrive_expect_tx(&full[s], kQ * bytes + S::kMaskBytes + (wrap_lo ? 48u : 0u) +
-                                          (wrap_hi ? 48u : 0u));
       unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
-      ST* stage = reinterpret_cast<ST*>(base);
-#pragma unroll
-      for (int i = 0; i < kQ; ++i) {
-        const ST* src = p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xs;
-        bulk_copy_g2s(stage + i * S::SROW + (xs - (tx0 - S::H)), src, bytes, &full[s]);
-      }
-      uint32_t* smask = reinterpret_cast<uint32_t*>(base + S::kPlaneBytes);
-      const int r3[3] = {ym, y, yp};
-#pragma unroll
-      for (int r = 0; r < 3; ++r)
-        bulk_copy_g2s(smask + r * S::MW, p.mask + static_cast<size_t>(r3[r]) * p.g.mask_words + (tx0 >> 5),
-                      S::MW * 4, &full[s]);
-      ST* wr = reinterpret_cast<ST*>(base + S::kPlaneBytes + S::kMaskBytes);
-      if (wrap_lo) {
-        const int xb = (nx - 1) & ~(S::H - 1);
-        for (int j = 0; j < 3; ++j) {
-          const int i = wrap_dir(j);
-          bulk_copy_g2s(wr + j * S::H,
-                        p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xb, 16,
-                        &full[s]);
-        }
-      }
-      if (wrap_hi) {
-        for (int j = 3; j < 6; ++j) {
-          const int i = wrap_dir(j);
-          bulk_copy_g2s(wr + j * S::H,
-                        p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch, 16,
-                        &full[s]);
-        }
-      }
+      tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
+        ring_issue_tile<ST, Phys, kOpen, S>(p, base, &full[s], y, tx0);
+      });
       if (++s == kStages) {
         s = 0;
         phase ^= 1u;
@@ -321,34 +357,10 @@ __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
   uint32_t phase = 0;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
     if (!mbar_wait_bounded_warp(&full[s], phase, err)) return;
-    const int tr = tile / tiles_per_row;
-    const int y = row0 + tr;
-    const int tx0 = (tile - tr * tiles_per_row) * S::TW;
-    const int xw = tx0 + cw * S::SW;
-    if (xw < nx) {
-      const unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
-      const ST* st = reinterpret_cast<const ST*>(base);
-      const uint32_t* sm = reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes);
-      const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes);
-      const int ym = y == 0 ? ny - 1 : y - 1;
-      const int yp = y == ny - 1 ? 0 : y + 1;
-      const int w0 = cw * S::WPS;  // first staged mask word of the strip
-      // Any solid among the strip's cells and their neighbours (words w0 .. w0 + WPS of 3 rows).
-      uint32_t mine = 0;
-      if (lane < 3 * (S::WPS + 1)) mine = sm[(lane / (S::WPS + 1)) * S::MW + w0 + lane % (S::WPS + 1)];
-      const bool solids = __any_sync(0xffffffffu, mine != 0u);
-#pragma unroll 1
-      for (int c = 0; c < kC; ++c) {
-        const int x = xw + 32 * S::LC * c + S::LC * lane;
-        if (x < nx) {
-          if constexpr (S::LC == 2)
-            ring_pair<ST, kOpen, S>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids);
-          else
-            ring_cell<ST, typename Phys::Arith, kOpen, S>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H,
-                                                         w0 + c, lane, solids);
-        }
-      }
-    }
+    const unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
+    tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
+      ring_consume_tile<ST, Phys, kOpen, S, kC>(p, base, y, tx0, cw, lane);
+    });
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
     if (++s == kStages) {
@@ -356,6 +368,27 @@ __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
       phase ^= 1u;
     }
   }
+}
+
+// Tiles of one grid: tiles_per_row tiles per row, rows row0, row0 + 1, ...
+template <class ST, class Phys, int kTW>
+struct GridTiles {
+  const StepArgs<ST, Phys>& p;
+  int tiles_per_row, row0;
+  template <class F>
+  __device__ __forceinline__ void visit(int tile, F&& f) const {
+    const int tr = tile / tiles_per_row;
+    f(p, row0 + tr, (tile - tr * tiles_per_row) * kTW);
+  }
+};
+
+template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
+__global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
+    ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int row0, int* err) {
+  using S = RingShape<ST, kW, kC>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  const GridTiles<ST, Phys, S::TW> grid_tiles{p, tiles_per_row, row0};
+  ring_pipeline<ST, Phys, kOpen, kW, kC, kStages>(smem, grid_tiles, tiles, err);
 }
 
 }  // namespace lbm_b200

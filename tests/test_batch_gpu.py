@@ -40,7 +40,7 @@ def test_sampled_instances_bit_exact(gpu_lib, orc, specs):
             assert np.array_equal(b.populations(k), want), f"instance {k} ({nx}x{ny})"
 
 
-@pytest.mark.parametrize("launch", [(0, 256, 0), (2, 128, 0), (4, 64, 300), (2, 256, 152)])
+@pytest.mark.parametrize("launch", [(0, 256, 0), (1, 256, 152), (2, 128, 0), (4, 64, 300), (2, 256, 152)])
 def test_batched_equals_separate_launches(gpu_lib, orc, specs, launch):
     with gpu_lib.Batch(specs) as a, gpu_lib.Batch(specs) as b:
         _fill(a, specs, orc)
@@ -102,5 +102,19 @@ def test_fp16_autotune_keeps_trajectory(gpu_lib, orc, specs, tmp_path):
         a.autotune(tmp_path / "tune16.txt")
         a.run(70)
         b.run(80)
+        for k in range(len(sub)):
+            assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k}"
+
+
+@pytest.mark.parametrize("shape", [(8, 2, 2), (4, 2, 4), (4, 1, 4), (2, 2, 2)])
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_ring_tile_shapes_equal_separate_launches(gpu_lib, orc, specs, shape, precision):
+    sub = specs[:12]
+    with gpu_lib.Batch(sub, precision=precision) as a, gpu_lib.Batch(sub, precision=precision) as b:
+        _fill(a, sub, orc)
+        _fill(b, sub, orc)
+        a.set_tiles(*shape)
+        a.run(70)
+        b.run_separate(70)
         for k in range(len(sub)):
             assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k}"
