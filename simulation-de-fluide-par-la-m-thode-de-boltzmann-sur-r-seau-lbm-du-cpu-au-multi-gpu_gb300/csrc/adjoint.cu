@@ -76,44 +76,6 @@ __global__ void adj_code_kernel(const uint32_t* __restrict__ mask, const AdjGeom
   }
 }
 
-// Forward collision of one cell with Brinkman drag, the reference's operand order under policy A
-// (src/v0_cpu/solver_v0.cpp:127-143 with F replaced by F_tot): writes the 9 post-collision
-// values through `store(i, value)` one direction at a time, so that no per-direction array stays
-// live; returns u_x (the objective's integrand).
-template <class A, class Store>
-__device__ __forceinline__ typename A::T cell_forward(const typename A::T (&yv)[kQ], typename A::T alpha,
-                                                      const AdjParams<typename A::T>& p, Store&& store) {
-  using T = typename A::T;
-  T m0 = T(0), mx = T(0), my = T(0);
-#pragma unroll
-  for (int i = 0; i < kQ; ++i) {
-    m0 = A::add(m0, yv[i]);
-    mx = A::add(mx, A::mul(T(dir_cx(i)), yv[i]));
-    my = A::add(my, A::mul(T(dir_cy(i)), yv[i]));
-  }
-  const T drho = m0;
-  const T rho = A::add(T(1), m0);
-  const T kf = A::add(T(1), A::mul(T(0.5), alpha));
-  const T d = A::mul(rho, kf);
-  const T ux = A::div(A::add(mx, p.hfx), d);
-  const T uy = A::div(A::add(my, p.hfy), d);
-  const T Fx = A::sub(p.fx, A::mul(A::mul(alpha, rho), ux));
-  const T Fy = A::sub(p.fy, A::mul(A::mul(alpha, rho), uy));
-  const T usq = A::add(A::mul(ux, ux), A::mul(uy, uy));
-#pragma unroll
-  for (int i = 0; i < kQ; ++i) {
-    const T cx = T(dir_cx(i)), cy = T(dir_cy(i)), w = weight<T>(i);
-    const T cu = A::add(A::mul(cx, ux), A::mul(cy, uy));
-    const T br = A::sub(A::add(A::mul(T(3), cu), A::mul(A::mul(T(4.5), cu), cu)), A::mul(T(1.5), usq));
-    const T geq = A::mul(w, A::add(drho, A::mul(rho, br)));
-    const T cf = A::add(A::mul(cx, Fx), A::mul(cy, Fy));
-    const T tf = A::add(A::mul(A::sub(cx, ux), Fx), A::mul(A::sub(cy, uy), Fy));
-    const T guo = A::mul(w, A::add(A::mul(T(3), tf), A::mul(A::mul(T(9), cu), cf)));
-    store(i, A::add(A::sub(yv[i], A::mul(p.omega, A::sub(yv[i], geq))), A::mul(p.fp, guo)));
-  }
-  return ux;
-}
-
 // Periodic neighbourhood of cell (x, y): column of x - 1, x, x + 1 and row offset (times nx) of
 // y - 1, y, y + 1, so that every gather index is one add.
 struct Nbhd {
@@ -191,6 +153,13 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
   const int b = blockIdx.y;
   const T* Rb = R + b * g.inst;
   T* Rnb = Rn ? Rn + b * g.inst : nullptr;
+  CollideConsts<T> k{};  // the collision's constants (cf_* unused: the force is per cell)
+  k.omega = p.omega;
+  k.force_prefactor = p.fp;
+  k.fx = p.fx;
+  k.fy = p.fy;
+  k.hfx = p.hfx;
+  k.hfy = p.hfy;
   T usum = T(0);  // per-thread partial sum (a few cells), added in double per block below
 #pragma unroll 1
   for (long long c = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; c < g.n;
@@ -204,12 +173,14 @@ __global__ void __launch_bounds__(kAdjThreads, 3)
       }
       continue;
     }
-    T yv[kQ];
+    T yv[kQ], out[kQ];
     gather_fwd(Rb, code, g, nbhd(g, x, y), static_cast<int>(c), yv);
     const T alpha = p.alpha ? p.alpha[b * g.n + c] : T(0);
-    const T ux = cell_forward<A>(yv, alpha, p, [&](int i, T v) {
-      if (write_out) Rnb[i * g.n + c] = v;
-    });
+    const T ux = collide_exact_drag<A>(yv, k, alpha, out);
+    if (write_out) {
+#pragma unroll
+      for (int i = 0; i < kQ; ++i) Rnb[i * g.n + c] = out[i];
+    }
     if (obj) usum += ux;
   }
   if (obj) block_add_to(static_cast<double>(usum), obj + b, smem);

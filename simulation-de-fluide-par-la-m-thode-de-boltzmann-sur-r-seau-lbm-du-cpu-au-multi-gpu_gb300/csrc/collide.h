@@ -76,13 +76,12 @@ inline CollideConsts<T> make_collide_consts(T tau, T fx, T fy) {
 // Only the sign of an exact zero can differ from v0 (numerically equal: the reference's tests
 // compare with `!=`). A state holding inf or NaN has diverged; results then differ from v0 only
 // in which non-finite value they hold.
+// Moments m0 = sum g, mx = sum c_x g, my = sum c_y g, sequential over i = 0..8 as in v0
+// (zero-coefficient terms dropped).
 template <class A>
-LBM_HD void collide_exact(const typename A::T (&g)[kQ], const CollideConsts<typename A::T>& k,
-                          typename A::T (&out)[kQ]) {
-  using T = typename A::T;
-  using S = typename A::S;
-  // Moments, sequential over i = 0..8 as in v0 (zero-coefficient terms dropped).
-  T m0 = g[0];
+LBM_HD void moments_seq(const typename A::T (&g)[kQ], typename A::T& m0, typename A::T& mx,
+                        typename A::T& my) {
+  m0 = g[0];
   m0 = A::add(m0, g[1]);
   m0 = A::add(m0, g[2]);
   m0 = A::add(m0, g[3]);
@@ -91,21 +90,27 @@ LBM_HD void collide_exact(const typename A::T (&g)[kQ], const CollideConsts<type
   m0 = A::add(m0, g[6]);
   m0 = A::add(m0, g[7]);
   m0 = A::add(m0, g[8]);
-  T mx = A::sub(g[1], g[3]);
+  mx = A::sub(g[1], g[3]);
   mx = A::add(mx, g[5]);
   mx = A::sub(mx, g[6]);
   mx = A::sub(mx, g[7]);
   mx = A::add(mx, g[8]);
-  T my = A::sub(g[2], g[4]);
+  my = A::sub(g[2], g[4]);
   my = A::add(my, g[5]);
   my = A::add(my, g[6]);
   my = A::sub(my, g[7]);
   my = A::sub(my, g[8]);
+}
 
-  const T drho = m0;
-  const T rho = A::add(A::k(S(1)), drho);
-  const T ux = A::div(A::add(mx, k.hfx), rho);
-  const T uy = A::div(A::add(my, k.hfy), rho);
+// Equilibrium, Guo source and BGK relaxation of one cell given its density, velocity and the
+// force acting on it (fx, fy; cf_p = fx + fy and cf_q = fy - fx, the c.F of directions 5 and 6).
+template <class A>
+LBM_HD void collide_exact_post(const typename A::T (&g)[kQ], typename A::T omega,
+                               typename A::T force_prefactor, typename A::T drho, typename A::T rho,
+                               typename A::T ux, typename A::T uy, typename A::T fx, typename A::T fy,
+                               typename A::T cf_p, typename A::T cf_q, typename A::T (&out)[kQ]) {
+  using T = typename A::T;
+  using S = typename A::S;
   const T usq = A::add(A::mul(ux, ux), A::mul(uy, uy));
   const T s15 = A::mul(A::k(S(1.5)), usq);
 
@@ -138,12 +143,12 @@ LBM_HD void collide_exact(const typename A::T (&g)[kQ], const CollideConsts<type
   for (int i = 1; i < kQ; ++i) geq[i] = A::mul(A::k(weight<S>(i)), A::add(drho, A::mul(rho, bracket[i])));
 
   // Guo source: t_i = (cx_i - ux) fx + (cy_i - uy) fy from six products, P_i = (9 cu_i) cf_i.
-  const T axp = A::mul(A::sub(A::k(S(1)), ux), k.fx);
-  const T axm = A::mul(A::sub(A::k(S(-1)), ux), k.fx);
-  const T ax0 = A::neg(A::mul(ux, k.fx));
-  const T ayp = A::mul(A::sub(A::k(S(1)), uy), k.fy);
-  const T aym = A::mul(A::sub(A::k(S(-1)), uy), k.fy);
-  const T ay0 = A::neg(A::mul(uy, k.fy));
+  const T axp = A::mul(A::sub(A::k(S(1)), ux), fx);
+  const T axm = A::mul(A::sub(A::k(S(-1)), ux), fx);
+  const T ax0 = A::neg(A::mul(ux, fx));
+  const T ayp = A::mul(A::sub(A::k(S(1)), uy), fy);
+  const T aym = A::mul(A::sub(A::k(S(-1)), uy), fy);
+  const T ay0 = A::neg(A::mul(uy, fy));
   T t[kQ];
   t[0] = A::add(ax0, ay0);
   t[1] = A::add(axp, ay0);
@@ -154,10 +159,10 @@ LBM_HD void collide_exact(const typename A::T (&g)[kQ], const CollideConsts<type
   t[6] = A::add(axm, ayp);
   t[7] = A::add(axm, aym);
   t[8] = A::add(axp, aym);
-  const T pa = A::mul(A::mul(nine, a), k.cf_x);
-  const T pb = A::mul(A::mul(nine, b), k.cf_y);
-  const T pp = A::mul(A::mul(nine, p), k.cf_p);
-  const T pq = A::mul(A::mul(nine, q), k.cf_q);
+  const T pa = A::mul(A::mul(nine, a), fx);
+  const T pb = A::mul(A::mul(nine, b), fy);
+  const T pp = A::mul(A::mul(nine, p), cf_p);
+  const T pq = A::mul(A::mul(nine, q), cf_q);
   T guo[kQ];
   guo[0] = A::mul(A::k(weight<S>(0)), A::mul(three, t[0]));
   guo[1] = A::mul(A::k(weight<S>(1)), A::add(A::mul(three, t[1]), pa));
@@ -173,8 +178,48 @@ LBM_HD void collide_exact(const typename A::T (&g)[kQ], const CollideConsts<type
 #pragma unroll
 #endif
   for (int i = 0; i < kQ; ++i)
-    out[i] = A::add(A::sub(g[i], A::mul(k.omega, A::sub(g[i], geq[i]))),
-                    A::mul(k.force_prefactor, guo[i]));
+    out[i] = A::add(A::sub(g[i], A::mul(omega, A::sub(g[i], geq[i]))), A::mul(force_prefactor, guo[i]));
+}
+
+template <class A>
+LBM_HD void collide_exact(const typename A::T (&g)[kQ], const CollideConsts<typename A::T>& k,
+                          typename A::T (&out)[kQ]) {
+  using T = typename A::T;
+  using S = typename A::S;
+  T m0, mx, my;
+  moments_seq<A>(g, m0, mx, my);
+  const T drho = m0;
+  const T rho = A::add(A::k(S(1)), drho);
+  const T ux = A::div(A::add(mx, k.hfx), rho);
+  const T uy = A::div(A::add(my, k.hfy), rho);
+  collide_exact_post<A>(g, k.omega, k.force_prefactor, drho, rho, ux, uy, k.cf_x, k.cf_y, k.cf_p,
+                        k.cf_q, out);
+}
+
+// The same collision with a Brinkman drag: the force on the cell is F_tot = F - alpha rho u and
+// the Guo velocity u = (m + F/2) / (rho (1 + alpha/2)) solves rho u = m + F_tot / 2; the
+// reference's literal order of these extra operations is kept (kf = 1 + 0.5 alpha, d = rho kf,
+// F_tot = F - (alpha rho) u), so alpha = 0 gives collide_exact's values (kf = 1, d = rho,
+// F_tot = F). Returns u_x.
+template <class A>
+LBM_HD typename A::T collide_exact_drag(const typename A::T (&g)[kQ], const CollideConsts<typename A::T>& k,
+                                        typename A::T alpha, typename A::T (&out)[kQ]) {
+  using T = typename A::T;
+  using S = typename A::S;
+  T m0, mx, my;
+  moments_seq<A>(g, m0, mx, my);
+  const T drho = m0;
+  const T rho = A::add(A::k(S(1)), drho);
+  const T kf = A::add(A::k(S(1)), A::mul(A::k(S(0.5)), alpha));
+  const T d = A::mul(rho, kf);
+  const T ux = A::div(A::add(mx, k.hfx), d);
+  const T uy = A::div(A::add(my, k.hfy), d);
+  const T ar = A::mul(alpha, rho);
+  const T fx = A::sub(k.fx, A::mul(ar, ux));
+  const T fy = A::sub(k.fy, A::mul(ar, uy));
+  collide_exact_post<A>(g, k.omega, k.force_prefactor, drho, rho, ux, uy, fx, fy, A::add(fx, fy),
+                        A::sub(fy, fx), out);
+  return ux;
 }
 
 // Moments of the reference's macroscopic() for one cell (src/v0_cpu/solver_v0.cpp:26-39,

@@ -1,6 +1,7 @@
 // Host check of the simplified exact collision (csrc/collide.h) against the literal collision
 // of the reference's v0 (src/v0_cpu/solver_v0.cpp:86-99,127-143, src/common/d2q9.hpp:40-50),
-// on random states, in float and double. Exit status 0 when every output value is equal.
+// on random states, in float and double, with and without the adjoint form's Brinkman drag
+// (collide_exact_drag). Exit status 0 when every output value is equal.
 // Compile with -ffp-contract=off.
 #include <cmath>
 #include <cstdio>
@@ -36,6 +37,33 @@ void literal(const T* g, T omega, T fp, T fx, T fy, T* out) {
   }
 }
 
+// The literal collision with a Brinkman drag (F_tot = F - (alpha rho) u, u = (m + F/2) / d,
+// d = rho (1 + 0.5 alpha)), the forward model of the adjoint form.
+template <class T>
+T literal_drag(const T* g, T omega, T fp, T fx, T fy, T alpha, T* out) {
+  T m0 = 0, mx = 0, my = 0;
+  for (int i = 0; i < 9; ++i) {
+    m0 += g[i];
+    mx += CX[i] * g[i];
+    my += CY[i] * g[i];
+  }
+  const T drho = m0, rho = T(1) + drho;
+  const T kf = T(1) + T(0.5) * alpha, d = rho * kf;
+  const T ux = (mx + T(0.5) * fx) / d, uy = (my + T(0.5) * fy) / d;
+  const T Fx = fx - (alpha * rho) * ux, Fy = fy - (alpha * rho) * uy;
+  const T usq = ux * ux + uy * uy;
+  for (int i = 0; i < 9; ++i) {
+    const T wi = lbm_b200::weight<T>(i);
+    const T cxi = T(CX[i]), cyi = T(CY[i]);
+    const T cu = cxi * ux + cyi * uy;
+    const T geq = wi * (drho + rho * (T(3) * cu + T(4.5) * cu * cu - T(1.5) * usq));
+    const T cf = cxi * Fx + cyi * Fy;
+    const T guo = wi * (T(3) * ((cxi - ux) * Fx + (cyi - uy) * Fy) + T(9) * cu * cf);
+    out[i] = g[i] - omega * (g[i] - geq) + fp * guo;
+  }
+  return ux;
+}
+
 template <class T>
 long check(long trials, unsigned seed) {
   std::mt19937_64 rng(seed);
@@ -58,6 +86,17 @@ long check(long trials, unsigned seed) {
       if (!(a[i] == b[i])) {
         if (bad < 5)
           std::printf("mismatch trial %ld dir %d: %.17g vs %.17g\n", t, i, (double)a[i], (double)b[i]);
+        ++bad;
+      }
+    // Brinkman drag (alpha in [0, 0.1], zero for some states)
+    const T alpha = t % 3 == 0 ? T(0) : T(0.05 + 0.05 * u(rng));
+    const T ua = literal_drag<T>(g, k.omega, k.force_prefactor, fx, fy, alpha, a);
+    const T ub = lbm_b200::collide_exact_drag<lbm_b200::HostArith<T>>(g, k, alpha, b);
+    if (!(ua == ub)) ++bad;
+    for (int i = 0; i < 9; ++i)
+      if (!(a[i] == b[i])) {
+        if (bad < 5)
+          std::printf("drag mismatch trial %ld dir %d: %.17g vs %.17g\n", t, i, (double)a[i], (double)b[i]);
         ++bad;
       }
     // moments
