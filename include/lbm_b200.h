@@ -214,6 +214,13 @@ int lbm_adj_get_populations(lbm_adjoint* a, int instance, void* s_host);
 /* Average device time of one forward step and of one backward step (recomputation included)
  * of the last runs, in seconds. */
 int lbm_adj_step_times(lbm_adjoint* a, double* forward_step_s, double* backward_step_s);
+/* Tile shape of the forward and backward kernels: cells per consumer lane, 1 (tiles of 256
+ * cells of a row) or 2 (512 cells, FP32 only), or 0 for the automatic choice (FP32 forward: the
+ * width leaving fewer idle lanes per row, the wider one on a tie; backward and FP64: 1). Results
+ * do not depend on it
+ * (forward bit for bit; gradients up to the order of their final FP64 sums). */
+int lbm_adj_set_tiles(lbm_adjoint* a, int forward_cells, int backward_cells);
+int lbm_adj_get_tiles(const lbm_adjoint* a, int* forward_cells, int* backward_cells);
 
 /* ---------------------------------------------------------------------------------------------
  * Batched ensemble (no counterpart in the reference): `count` independent closed channels of

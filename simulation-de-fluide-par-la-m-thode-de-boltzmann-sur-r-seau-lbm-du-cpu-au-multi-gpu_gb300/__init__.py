@@ -92,6 +92,8 @@ def lib() -> C.CDLL:
             "lbm_adj_backward": ([vp, vp, vp, vp, vp], i),
             "lbm_adj_get_populations": ([vp, i, vp], i),
             "lbm_adj_step_times": ([vp, C.POINTER(d), C.POINTER(d)], i),
+            "lbm_adj_set_tiles": ([vp, i, i], i),
+            "lbm_adj_get_tiles": ([vp, C.POINTER(i), C.POINTER(i)], i),
             "lbm_batch_create": ([i, vp, vp, vp, vp, vp, vp, i, C.POINTER(vp)], i),
             "lbm_batch_destroy": ([vp], i),
             "lbm_batch_last_error": ([vp], C.c_char_p),
@@ -359,6 +361,16 @@ class Adjoint:
     def step_times(self):
         f, b = C.c_double(), C.c_double()
         self._check(lib().lbm_adj_step_times(self._h, C.byref(f), C.byref(b)))
+        return f.value, b.value
+
+    def set_tiles(self, forward_cells=0, backward_cells=0):
+        """Cells per consumer lane of the forward / backward kernels: 1 (256-cell tiles), 2
+        (512-cell tiles, FP32 only) or 0 (automatic). Results do not depend on it."""
+        self._check(lib().lbm_adj_set_tiles(self._h, forward_cells, backward_cells))
+
+    def tiles(self):
+        f, b = C.c_int(), C.c_int()
+        self._check(lib().lbm_adj_get_tiles(self._h, C.byref(f), C.byref(b)))
         return f.value, b.value
 
 

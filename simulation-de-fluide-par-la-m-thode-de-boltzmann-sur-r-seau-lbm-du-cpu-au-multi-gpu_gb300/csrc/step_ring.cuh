@@ -303,13 +303,17 @@ __device__ __forceinline__ void ring_consume_tile(const StepArgs<ST, Phys>& p, c
   }
 }
 
-// The warp-specialised pipeline over tiles 0 .. tiles - 1, grid-stride: `tiles_of.visit(tile, f)`
-// calls f(p, y, tx0) with the grid, row and first cell of a tile (one grid for the solver, the
-// tile's instance for the batched ensemble).
-template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, class Tiles>
-__device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& tiles_of, int tiles, int* err) {
-  using S = RingShape<ST, kW, kC>;
-  uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);
+// Warp-specialised pipeline over tiles 0 .. tiles - 1 (grid-stride) with a ring of kStages
+// stages of kStageBytes: warp 0 (one lane) calls pol.issue(tile, stage, full_barrier), which
+// arms the barrier with its byte count and issues the bulk copies; consumer warps 1 .. kW wait
+// for the stage, call pol.consume(tile, stage, consumer_warp, lane) and release it. Waits are
+// bounded (error flag). Afterwards every consumer warp (not the producer) calls
+// pol.finish(cw, lane), also after a wait ran out (the host then reports the timeout), e.g. to
+// write the warp's partial sums. Warps never synchronise with one another after the start, so
+// a wait that ran out in one warp cannot leave another waiting at a barrier.
+template <int kW, int kStages, int kStageBytes, class Pol>
+__device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int tiles, int* err) {
+  uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * kStageBytes);
   uint64_t* empty = full + kStages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (threadIdx.x == 0) {
@@ -332,10 +336,7 @@ __device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& 
         ok = false;
         break;
       }
-      unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
-      tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
-        ring_issue_tile<ST, Phys, kOpen, S>(p, base, &full[s], y, tx0);
-      });
+      pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s]);
       if (++s == kStages) {
         s = 0;
         phase ^= 1u;
@@ -356,11 +357,8 @@ __device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& 
   int s = 0;
   uint32_t phase = 0;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    if (!mbar_wait_bounded_warp(&full[s], phase, err)) return;
-    const unsigned char* base = smem + static_cast<size_t>(s) * S::kStageBytes;
-    tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
-      ring_consume_tile<ST, Phys, kOpen, S, kC>(p, base, y, tx0, cw, lane);
-    });
+    if (!mbar_wait_bounded_warp(&full[s], phase, err)) break;
+    pol.consume(tile, smem + static_cast<size_t>(s) * kStageBytes, cw, lane);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
     if (++s == kStages) {
@@ -368,6 +366,35 @@ __device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& 
       phase ^= 1u;
     }
   }
+  if (Pol::kFinish) pol.finish(cw, lane);
+}
+
+// The step pipeline of one tile visitor (`tiles_of.visit(tile, f)` calls f(p, y, tx0) with the
+// grid, row and first cell of a tile: one grid for the solver, the tile's instance for the
+// batched ensemble).
+template <class ST, class Phys, bool kOpen, int kW, int kC, class Tiles>
+struct StepPolicy {
+  using S = RingShape<ST, kW, kC>;
+  static constexpr bool kFinish = false;
+  const Tiles& tiles_of;
+  __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full) const {
+    tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
+      ring_issue_tile<ST, Phys, kOpen, S>(p, base, full, y, tx0);
+    });
+  }
+  __device__ __forceinline__ void consume(int tile, const unsigned char* base, int cw, int lane) const {
+    tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
+      ring_consume_tile<ST, Phys, kOpen, S, kC>(p, base, y, tx0, cw, lane);
+    });
+  }
+  __device__ __forceinline__ void finish(int, int) const {}
+};
+
+template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, class Tiles>
+__device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& tiles_of, int tiles, int* err) {
+  using S = RingShape<ST, kW, kC>;
+  StepPolicy<ST, Phys, kOpen, kW, kC, Tiles> pol{tiles_of};
+  tile_pipeline<kW, kStages, S::kStageBytes>(smem, pol, tiles, err);
 }
 
 // Tiles of one grid: tiles_per_row tiles per row, rows row0, row0 + 1, ...

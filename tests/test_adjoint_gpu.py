@@ -148,3 +148,90 @@ def test_autograd_wrapper(setup, adjoint64):
     assert float(fx.grad) == pytest.approx(2.0 * g64["fx"][0], rel=1e-10)
     assert float(tau.grad) == pytest.approx(2.0 * g64["tau"][0], rel=1e-10)
     np.testing.assert_allclose(al.grad.numpy()[cells], 2.0 * g64["alpha"][0][cells], rtol=1e-9)
+
+
+# Ragged geometry: nx = 300 is not a multiple of the 256- or 512-cell tiles (partial last tile,
+# row padding to the pitch), a disc across the x = 256 tile boundary and one across the periodic
+# x wrap exercise bounce-back in both gathers at tile edges.
+RNX, RNY = 300, 64
+
+
+def _ragged(pkg):
+    geo = pkg.geometry
+    mask = pkg.workloads.adjoint_channel(RNX, RNY)
+    mask = geo.add_disc(mask, RNX, RNY, 255.0, 30.0, 12.0)
+    mask = geo.add_disc(mask, RNX, RNY, 3.0, 40.0, 8.0)
+    alpha = pkg.workloads.brinkman_field(RNX, RNY, seed=99, wmin=4.0, wmax=12.0)
+    alpha[mask != 0] = 0.0
+    return mask.astype(np.uint8), alpha
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("cells", [1, 2])
+def test_ragged_zero_alpha_is_plain_method(gpu_lib, orc, precision, cells):
+    pkg = gpu_lib
+    if precision == "fp64" and cells == 2:
+        pytest.skip("two cells per lane is an FP32 tile shape")
+    mask, _ = _ragged(pkg)
+    real = "f32" if precision == "fp32" else "f64"
+    s0 = orc.seeded_state(5, 1e-3, RNX, RNY, mask, real)
+    with pkg.Adjoint(RNX, RNY, TAU, FX, 0.0, mask, precision=precision, checkpoint_every=40) as a:
+        a.set_tiles(cells, cells)
+        assert a.tiles() == (cells, cells)
+        a.forward(120, 1, s0=s0)
+        got = a.populations(0)
+    with pkg.Solver(RNX, RNY, TAU, FX, 0.0, mask, precision=precision) as s:
+        s.set_populations(s0)
+        s.run(120)
+        want = s.populations()
+    assert np.array_equal(got, want)
+
+
+def test_tile_shapes_agree(gpu_lib):
+    """Both tile shapes of both sweeps: the same states and per-cell gradients bit for bit (the
+    per-cell recursions do not depend on the tiling), the same objective and parameter
+    gradients up to the order of their sums."""
+    pkg = gpu_lib
+    mask, alpha = _ragged(pkg)
+    results = {}
+    for shape in [(1, 1), (2, 2), (1, 2), (2, 1)]:
+        with pkg.Adjoint(RNX, RNY, TAU, FX, 0.0, mask, precision="fp32", batch=2, checkpoint_every=70) as a:
+            a.set_tiles(*shape)
+            a.set_alpha(np.stack([alpha, 0.5 * alpha]))
+            J = a.forward(500, 60)
+            g = a.backward()
+            results[shape] = (J, g, a.populations(1))
+    J0, g0, s0 = results[(1, 1)]
+    for shape, (J, g, s) in results.items():
+        assert np.array_equal(s, s0), shape
+        np.testing.assert_allclose(J, J0, rtol=1e-5)
+        assert np.array_equal(g["alpha"], g0["alpha"]), shape
+        np.testing.assert_allclose(g["fx"], g0["fx"], rtol=1e-5)
+        np.testing.assert_allclose(g["tau"], g0["tau"], rtol=1e-5)
+
+
+def test_ragged_gradient_matches_finite_differences(gpu_lib):
+    """FP64 at the ragged size, checkpoints every 70 of 600 steps (a short last segment): the
+    gradients with respect to fx and to the alpha cell of largest drag agree with central
+    differences to 1e-4 relative."""
+    pkg = gpu_lib
+    mask, alpha = _ragged(pkg)
+    steps, window = 600, 100
+
+    def J(fx, al):
+        with pkg.Adjoint(RNX, RNY, TAU, fx, 0.0, mask, precision="fp64", checkpoint_every=steps) as a:
+            a.set_alpha(al)
+            return a.forward(steps, window)[0]
+
+    with pkg.Adjoint(RNX, RNY, TAU, FX, 0.0, mask, precision="fp64", checkpoint_every=70) as a:
+        a.set_alpha(alpha)
+        a.forward(steps, window)
+        g = a.backward()
+    h = FD_REL * FX
+    assert g["fx"][0] == pytest.approx((J(FX + h, alpha) - J(FX - h, alpha)) / (2 * h), rel=1e-4)
+    c = int(np.argmax(alpha))
+    ap, am = alpha.copy(), alpha.copy()
+    ap[c] += FD_REL * alpha[c]
+    am[c] -= FD_REL * alpha[c]
+    d_a = (J(FX, ap) - J(FX, am)) / (2 * FD_REL * alpha[c])
+    assert g["alpha"][0][c] == pytest.approx(d_a, rel=1e-4)

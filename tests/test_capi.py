@@ -76,6 +76,19 @@ def test_collision_algebra_on_host(tmp_path, orc):
 
 
 @pytest.mark.skipif(shutil.which("g++") is None, reason="no host compiler")
+def test_fastdiv_on_host(tmp_path):
+    """csrc/fastdiv.h (the tile decoders' division by invariant integers) equals integer
+    division on edge and random dividends for divisors 1..4096 and large ones."""
+    src = ROOT / "tests" / "cpp" / "fastdiv_test.cpp"
+    exe = tmp_path / "fastdiv_test"
+    pkgdir = next(ROOT.glob("simulation-de-fluide-*_gb300"))
+    subprocess.run(["g++", "-std=c++17", "-O2", "-I", str(pkgdir / "csrc"), str(src), "-o", str(exe)],
+                   check=True)
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.skipif(shutil.which("g++") is None, reason="no host compiler")
 def test_cpp_wrapper_compiles(tmp_path):
     """include/lbm_b200.hpp (the SolverV3 drop-in) compiles standalone against the C header."""
     src = tmp_path / "w.cpp"
