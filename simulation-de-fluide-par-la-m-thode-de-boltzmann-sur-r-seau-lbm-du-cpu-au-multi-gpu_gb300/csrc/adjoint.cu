@@ -268,6 +268,14 @@ __device__ __forceinline__ void issue_pull(unsigned char* st, unsigned char* wra
   }
 }
 
+// Programmatic dependent launch: wait until the previous kernel on the stream has completed and
+// its writes are visible (a no-op when the kernel was launched without the attribute), then let
+// the next kernel's blocks be scheduled as this one's exit.
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 // Warp sum (fixed shuffle tree) of one value per lane, added by lane 0 to *slot.
 __device__ __forceinline__ void warp_add_to(double v, double* slot, int lane) {
 #pragma unroll
@@ -371,6 +379,7 @@ template <class A, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(kAdjThreads, kMinBlocks)
     adj_forward_kernel(const FwdArgs<typename A::T> p, int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
   AdjForward<A, kC> pol{p};
   tile_pipeline<kAdjW, kStages, FwdStage<typename A::T, kC>::kBytes>(smem, pol, p.at.total, err);
 }
@@ -617,6 +626,7 @@ template <class T, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(kAdjThreads, kMinBlocks)
     adj_backward_kernel(const BwdArgs<T> p, int* err) {
   extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
   AdjBackward<T, kC> pol{p};
   tile_pipeline<kAdjW, kStages, BwdStage<T, kC>::kBytes>(smem, pol, p.at.total, err);
 }
@@ -734,7 +744,7 @@ struct lbm_adjoint {
   void* state[2] = {nullptr, nullptr};
   void* ckpt = nullptr;          // checkpoints: (T/K + 1) states
   size_t ckpt_count = 0;
-  void* seg = nullptr;           // K + 1 recomputed states
+  void* seg = nullptr;           // K recomputed states (a segment's first state is its checkpoint)
   void* ybar[2] = {nullptr, nullptr};
   double* abar = nullptr;        // batch pitched planes
   void* aseg = nullptr;          // batch pitched planes, per-segment alpha_bar in the state precision
@@ -749,7 +759,7 @@ struct lbm_adjoint {
   void* stage = nullptr;
   size_t stage_bytes = 0;
   int steps = 0, window = 0;     // of the last forward
-  int fin_state = 0;             // state[] index holding R_T after the forward
+  const void* fin = nullptr;     // R_T after the forward (a state buffer or a checkpoint slot)
   bool have_forward = false;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
@@ -892,26 +902,43 @@ FwdArgs<typename A::T> fwd_args(const lbm_adjoint* a) {
   return p;
 }
 
+// Launch of a ring kernel with programmatic stream serialisation: its blocks may be scheduled
+// while the previous kernel on the stream drains; they wait (griddepcontrol.wait) for its
+// completion and memory before touching any buffer.
+template <class K, class Args>
+int launch_ring(lbm_adjoint* a, K kernel, int grid, size_t smem, const Args& p) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3(grid);
+  cfg.blockDim = dim3(kAdjThreads);
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = a->stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  ADJ_CUDA(a, cudaLaunchKernelEx(&cfg, kernel, p, a->err_d));
+  return LBM_OK;
+}
+
 template <class A>
-void launch_forward(lbm_adjoint* a, FwdArgs<typename A::T> p, const void* R, void* Rn, double* obj) {
+int launch_forward(lbm_adjoint* a, FwdArgs<typename A::T> p, const void* R, void* Rn, double* obj) {
   using T = typename A::T;
   p.R = static_cast<const T*>(R);
   p.Rn = static_cast<T*>(Rn);
   p.obj = obj;
-  with_shape<T>(a->fwd_c, [&](auto kc) {
+  return with_shape<T>(a->fwd_c, [&](auto kc) {
     constexpr int kC = decltype(kc)::value;
-    AdjKernels<A, kC>::fwd<<<a->fwd_grid, kAdjThreads, AdjLaunch<T, kC>::fwd_smem(), a->stream>>>(p, a->err_d);
-    return 0;
+    return launch_ring(a, AdjKernels<A, kC>::fwd, a->fwd_grid, AdjLaunch<T, kC>::fwd_smem(), p);
   });
 }
 
 template <class A>
-void launch_backward(lbm_adjoint* a, const BwdArgs<typename A::T>& p) {
+int launch_backward(lbm_adjoint* a, const BwdArgs<typename A::T>& p) {
   using T = typename A::T;
-  with_shape<T>(a->bwd_c, [&](auto kc) {
+  return with_shape<T>(a->bwd_c, [&](auto kc) {
     constexpr int kC = decltype(kc)::value;
-    AdjKernels<A, kC>::bwd<<<a->bwd_grid, kAdjThreads, AdjLaunch<T, kC>::bwd_smem(), a->stream>>>(p, a->err_d);
-    return 0;
+    return launch_ring(a, AdjKernels<A, kC>::bwd, a->bwd_grid, AdjLaunch<T, kC>::bwd_smem(), p);
   });
 }
 
@@ -945,6 +972,9 @@ int forward_t(lbm_adjoint* a, const void* s0_host, int steps, int window, double
     ADJ_CUDA(a, cudaMalloc(&a->ckpt, nckpt * sb));
     a->ckpt_count = nckpt;
   }
+  // Checkpoint slot k holds R_{kK}; the forward writes checkpoint steps straight into their slot
+  // and the other steps into the two state buffers alternately.
+  char* ckpt = static_cast<char*>(a->ckpt);
   if (s0_host) {
     const size_t hb = static_cast<size_t>(a->batch) * kQ * a->g.nx * a->g.ny * sizeof(T);
     if (a->stage_bytes < hb) {
@@ -955,25 +985,25 @@ int forward_t(lbm_adjoint* a, const void* s0_host, int steps, int window, double
     }
     ADJ_CUDA(a, cudaMemcpyAsync(a->stage, s0_host, hb, cudaMemcpyHostToDevice, a->stream));
     adj_set_state_kernel<T><<<dim3(2 * a->sm_count, a->batch), kAuxThreads, 0, a->stream>>>(
-        static_cast<T*>(a->state[0]), a->mask_d, a->g, static_cast<const T*>(a->stage));
+        reinterpret_cast<T*>(ckpt), a->mask_d, a->g, static_cast<const T*>(a->stage));
   } else {
-    ADJ_CUDA(a, cudaMemsetAsync(a->state[0], 0, sb, a->stream));  // rest: f_i - w_i = 0
+    ADJ_CUDA(a, cudaMemsetAsync(ckpt, 0, sb, a->stream));  // rest: f_i - w_i = 0
   }
-  ADJ_CUDA(a, cudaMemcpyAsync(a->ckpt, a->state[0], sb, cudaMemcpyDeviceToDevice, a->stream));
   ADJ_CUDA(a, cudaMemsetAsync(a->obj_part, 0, a->obj_slots * sizeof(double), a->stream));
   const FwdArgs<T> p = fwd_args<A>(a);
-  int cur = 0;
+  const void* cur = ckpt;
+  int spare = 0;
   ADJ_CUDA(a, cudaEventRecord(a->ev[0], a->stream));
   for (int t = 0; t < steps; ++t) {
     const bool in_window = t >= steps - window + 1;
-    launch_forward<A>(a, p, a->state[cur], a->state[cur ^ 1], in_window ? a->obj_part : nullptr);
-    cur ^= 1;
-    if ((t + 1) % a->K == 0)
-      ADJ_CUDA(a, cudaMemcpyAsync(static_cast<char*>(a->ckpt) + ((t + 1) / a->K) * sb,
-                                  a->state[cur], sb, cudaMemcpyDeviceToDevice, a->stream));
+    const bool is_ckpt = (t + 1) % a->K == 0;
+    void* out = is_ckpt ? ckpt + static_cast<size_t>((t + 1) / a->K) * sb : a->state[spare];
+    if (const int rc = launch_forward<A>(a, p, cur, out, in_window ? a->obj_part : nullptr)) return rc;
+    if (!is_ckpt) spare ^= 1;
+    cur = out;
   }
   ADJ_CUDA(a, cudaEventRecord(a->ev[1], a->stream));
-  launch_forward<A>(a, p, a->state[cur], nullptr, a->obj_part);  // objective of the final state
+  if (const int rc = launch_forward<A>(a, p, cur, nullptr, a->obj_part)) return rc;  // final state's objective
   ADJ_CUDA(a, cudaGetLastError());
   std::vector<double> sums;
   if (const int rc = read_sums(a, a->obj_part, a->fwd_grid, 1, sums)) return rc;
@@ -984,7 +1014,7 @@ int forward_t(lbm_adjoint* a, const void* s0_host, int steps, int window, double
   a->steps = steps;
   a->window = window;
   a->have_forward = true;
-  a->fin_state = cur;
+  a->fin = cur;
   return LBM_OK;
 }
 
@@ -995,8 +1025,8 @@ int backward_t(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* d
   const size_t sb = state_bytes(a);
   const int T_steps = a->steps, W = a->window, K = a->K;
   if (!a->seg) {
-    ADJ_CUDA(a, cudaMalloc(&a->seg, (K + 1) * sb));
-    ADJ_CUDA(a, cudaMemsetAsync(a->seg, 0, (K + 1) * sb, a->stream));
+    ADJ_CUDA(a, cudaMalloc(&a->seg, static_cast<size_t>(K) * sb));
+    ADJ_CUDA(a, cudaMemsetAsync(a->seg, 0, static_cast<size_t>(K) * sb, a->stream));
   }
   for (int k = 0; k < 2; ++k)
     if (!a->ybar[k]) {
@@ -1032,21 +1062,21 @@ int backward_t(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* d
   const int nseg = (T_steps + K - 1) / K;
   for (int s = nseg - 1; s >= 0; --s) {
     const int t0 = s * K, t1 = std::min(T_steps, t0 + K);
-    // Recompute R_{t0..t1} from checkpoint s.
-    ADJ_CUDA(a, cudaMemcpyAsync(seg, static_cast<char*>(a->ckpt) + static_cast<size_t>(s) * sb, sb,
-                                cudaMemcpyDeviceToDevice, a->stream));
+    // R_{t0} is checkpoint s; recompute R_{t0 + 1 .. t1} into seg[0 .. t1 - t0 - 1].
+    const char* base = static_cast<const char*>(a->ckpt) + static_cast<size_t>(s) * sb;
+    auto state_at = [&](int t) -> const void* { return t == t0 ? base : seg + static_cast<size_t>(t - t0 - 1) * sb; };
     for (int t = t0; t < t1; ++t)
-      launch_forward<A>(a, pf, seg + (t - t0) * sb, seg + (t - t0 + 1) * sb, nullptr);
+      if (const int rc = launch_forward<A>(a, pf, state_at(t), seg + static_cast<size_t>(t - t0) * sb, nullptr)) return rc;
     // Adjoint steps t1 (only for the last segment: the final state) .. t0.
     const int top = (s == nseg - 1) ? t1 : t1 - 1;
     for (int t = top; t >= t0; --t) {
       const bool in_window = t >= T_steps - W + 1;
-      pb.R = reinterpret_cast<const T*>(seg + (t - t0) * sb);
+      pb.R = static_cast<const T*>(state_at(t));
       pb.Z = first ? nullptr : static_cast<const T*>(a->ybar[yb ^ 1]);
       pb.Yb = static_cast<T*>(a->ybar[yb]);
       pb.obj_coef = in_window ? coef : T(0);
       pb.flush = t == t0 ? 1 : 0;
-      launch_backward<A>(a, pb);
+      if (const int rc = launch_backward<A>(a, pb)) return rc;
       first = false;
       yb ^= 1;
     }
@@ -1081,7 +1111,7 @@ int get_state_t(lbm_adjoint* a, int b, void* host) {
     a->stage_bytes = bytes;
   }
   adj_get_state_kernel<T><<<2 * a->sm_count, kAuxThreads, 0, a->stream>>>(
-      static_cast<const T*>(a->state[a->fin_state]), a->mask_d, a->g, b, static_cast<T*>(a->stage));
+      static_cast<const T*>(a->fin), a->mask_d, a->g, b, static_cast<T*>(a->stage));
   ADJ_CUDA(a, cudaMemcpyAsync(host, a->stage, bytes, cudaMemcpyDeviceToHost, a->stream));
   ADJ_CUDA(a, cudaStreamSynchronize(a->stream));
   return LBM_OK;
