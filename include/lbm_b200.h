@@ -168,7 +168,9 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * (16-bit storage) per lane, consecutive lanes on consecutive cells: 12 = 8 consumer warps,
  * 2 passes per strip, 2 stages; 13 = the same with 3 stages; 14 = 12 capped at 56 registers for
  * 4 resident blocks; 15 = 4 consumer warps, 3 stages; 16 = 15 capped for 7 resident blocks;
- * 17 = 12 capped for 3 resident blocks.
+ * 17 = 12 capped for 3 resident blocks; 18 = 17 with 3 stages; 19 = 17 with 1 pass per strip
+ * (half-width tiles) and 4 stages. The ring variants are launched with programmatic stream
+ * serialisation (the next step's blocks are scheduled while the previous step drains).
  * -1 (the default): 12 (plain FP32 / FP64, 512-cell tiles) or 17 (16-bit storage, 1024-cell
  * tiles) when there are at least two tiles per SM, 0 otherwise.
  * The 16-bit forms round stored populations stochastically (see lbm_create); every variant

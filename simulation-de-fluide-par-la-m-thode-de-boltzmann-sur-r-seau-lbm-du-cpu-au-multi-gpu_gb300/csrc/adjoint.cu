@@ -268,14 +268,6 @@ __device__ __forceinline__ void issue_pull(unsigned char* st, unsigned char* wra
   }
 }
 
-// Programmatic dependent launch: wait until the previous kernel on the stream has completed and
-// its writes are visible (a no-op when the kernel was launched without the attribute), then let
-// the next kernel's blocks be scheduled as this one's exit.
-__device__ __forceinline__ void grid_dependency_wait() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
 // Warp sum (fixed shuffle tree) of one value per lane, added by lane 0 to *slot.
 __device__ __forceinline__ void warp_add_to(double v, double* slot, int lane) {
 #pragma unroll
@@ -902,22 +894,9 @@ FwdArgs<typename A::T> fwd_args(const lbm_adjoint* a) {
   return p;
 }
 
-// Launch of a ring kernel with programmatic stream serialisation: its blocks may be scheduled
-// while the previous kernel on the stream drains; they wait (griddepcontrol.wait) for its
-// completion and memory before touching any buffer.
 template <class K, class Args>
 int launch_ring(lbm_adjoint* a, K kernel, int grid, size_t smem, const Args& p) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = dim3(grid);
-  cfg.blockDim = dim3(kAdjThreads);
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = a->stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  ADJ_CUDA(a, cudaLaunchKernelEx(&cfg, kernel, p, a->err_d));
+  ADJ_CUDA(a, launch_dependent(kernel, dim3(grid), dim3(kAdjThreads), smem, a->stream, p, a->err_d));
   return LBM_OK;
 }
 

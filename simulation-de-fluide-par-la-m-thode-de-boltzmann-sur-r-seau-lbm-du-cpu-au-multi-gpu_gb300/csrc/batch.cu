@@ -6,9 +6,9 @@
 // walk the global chunk list (chunks of 32 * G cells of one row of one instance), find their
 // instance by binary search over the first-chunk indices staged in shared memory, and run the
 // same chunk code as the single-grid kernel (step_kernel.cuh). The default kernel is instead the
-// warp-specialised ring of the single-grid solver (step_ring.cuh) over the ensemble's tiles: a
-// tile's instance comes from a binary search over the per-instance first-tile indices staged in
-// shared memory. Steps are replayed from a CUDA graph of kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
+// warp-specialised ring of the single-grid solver (step_ring.cuh) over the ensemble's tiles of
+// consecutive row strips (a tile may cover several short rows): a tile's instance comes from a
+// binary search over the per-instance first-tile indices staged in shared memory. Steps are replayed from a CUDA graph of kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
 // instance per step (the comparison point). lbm_batch_autotune() times the candidate launch
 // shapes (cells per thread G, i.e. the chunk width 32 G, threads per block, blocks per SM) on the
 // actual ensemble and keeps the fastest, caching the choice per GPU, form and ensemble size.
@@ -28,6 +28,7 @@
 #include "lbm_b200.h"
 #include "solver_internal.h"
 #include "forms.cuh"
+#include "fastdiv.h"
 #include "step_kernel.cuh"
 #include "step_ring.cuh"
 
@@ -39,14 +40,17 @@ constexpr int kBatchThreads = 256;
 constexpr int kBatchMaxInstances = 4096;  // first-chunk indices staged in shared memory
 constexpr int kGraphSteps = 64;
 
+// One instance of the table (16-byte aligned and sized: the ring kernel's producer copies a tile's
+// entry into the tile's stage).
 template <class Consts>
-struct BatchInst {
+struct alignas(16) BatchInst {
   long long off;       // element offset of the instance's planes in a state buffer
   long long mask_off;  // word offset of its mask rows
   Grid2D g;
   int cpr;     // chunks per row for the launch's G
   int item0;   // first global chunk index
-  int tpr;     // ring tiles per row
+  int spr;     // ring strips per row (strips of the tile shape's strip width)
+  FastDiv spr_div;
   int tile0;   // first global ring tile index
   Consts k;
 };
@@ -106,14 +110,65 @@ __global__ void __launch_bounds__(kBatchThreads)
   }
 }
 
-// Tiles of the ensemble for the ring pipeline: instance by binary search over the first-tile
-// indices in shared memory, then that instance's grid from the table.
-template <class ST, class Phys, int kTW>
-struct BatchTiles {
+// Ring tiles of the ensemble. An instance's rows are cut into strips of SW = 32 kC LC cells (one
+// consumer warp's share of a tile, LC = 2 for the 16-bit pairs); its strips are numbered row by
+// row, and a tile is kW consecutive strips of one instance. A tile therefore covers several
+// whole rows of a narrow instance or straddles two rows of a wide one, and every consumer warp
+// has a strip unless the instance's last tile is short: on the benchmark ensemble (row widths
+// 65..1020) 94 % of the lanes of the FP32 8 x 2 shape hold a cell, against 69 % for tiles of one
+// row segment each.
+//
+// Stage layout: the tile's rows are segments g = 0 .. nseg - 1 (nseg <= kW). Plane i holds, for
+// each segment, its cells plus a 16-byte halo on each side, segments one after the other: the
+// strip of consumer warp w, in segment g, starts at element w SW + (2 g + 1) H of the plane's
+// SROW elements. Per segment the stage also holds the 3 mask rows around it (MW words each, from
+// the 16-byte-aligned word below the segment's first cell) and its 6 wrap blocks.
+template <class ST, int kW, int kC>
+struct FlatShape {
+  using R = RingShape<ST, kW, kC>;
+  static constexpr int H = R::H, LC = R::LC, SW = R::SW, WPS = R::WPS, TW = R::TW;
+  static constexpr int SROW = TW + 2 * H * kW;
+  static constexpr int MW = TW / 32 + 4;
+  static constexpr int kPlaneBytes = kQ * SROW * static_cast<int>(sizeof(ST));
+  static constexpr int kMaskBytes = kW * 3 * MW * 4;
+  static constexpr int kWrapBytes = kW * 6 * 16;
+  static constexpr int kStageBytes = kPlaneBytes + kMaskBytes + kWrapBytes;
+  static constexpr int kThreads = 32 * (kW + 1);
+  static_assert(SW % 32 == 0 && (SROW * static_cast<int>(sizeof(ST))) % 16 == 0 && kStageBytes % 16 == 0,
+                "stage parts must stay 16-byte aligned");
+};
+
+// Segment g of a tile whose strips are s0 .. s1 - 1 (row ya = s0 / spr first): its row and its
+// first and last strip in that row.
+struct Segment {
+  int y, j_lo, j_hi, w_first;
+};
+__device__ __forceinline__ Segment tile_segment(int g, int s0, int s1, int ya, int spr) {
+  Segment sg;
+  sg.y = ya + g;
+  const int row_s = sg.y * spr;
+  sg.j_lo = s0 > row_s ? s0 - row_s : 0;
+  sg.j_hi = (s1 - 1 < row_s + spr - 1 ? s1 - 1 : row_s + spr - 1) - row_s;
+  sg.w_first = row_s + sg.j_lo - s0;
+  return sg;
+}
+
+// Stage of the batch ring: the tile's rows, masks and wrap blocks (FlatShape), then the table
+// entry of the tile's instance, copied by the producer with the rest, so that the consumers
+// neither search the table nor wait on global loads of it.
+template <class ST, class Phys, int kW, int kC>
+struct BatchFlatPolicy {
+  using S = FlatShape<ST, kW, kC>;
+  using Inst = BatchInst<typename Phys::Consts>;
+  static constexpr bool kFinish = false;
+  static constexpr bool kWarpIssue = true;
+  static constexpr int kInstBytes = static_cast<int>(sizeof(Inst));
+  static constexpr int kStageBytes = S::kStageBytes + kInstBytes;
+  static_assert(kInstBytes % 16 == 0, "table entries are copied in 16-byte units");
   const BatchArgs<ST, Phys>& a;
   const int* s_tile0;
-  template <class F>
-  __device__ __forceinline__ void visit(int tile, F&& f) const {
+
+  __device__ __forceinline__ int instance_of(int tile) const {
     int lo = 0, hi = a.count - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -122,7 +177,10 @@ struct BatchTiles {
       else
         hi = mid - 1;
     }
-    const BatchInst<typename Phys::Consts>& d = a.inst[lo];
+    return lo;
+  }
+
+  __device__ __forceinline__ StepArgs<ST, Phys> grid_of(const Inst& d) const {
     StepArgs<ST, Phys> p;
     p.src = a.src + d.off;
     p.dst = a.dst + d.off;
@@ -133,11 +191,127 @@ struct BatchTiles {
     p.step_ctr = a.step;
     p.step_off = 0;
     p.key_base = d.off / kQ;
-    const int local = tile - s_tile0[lo];
-    const int tr = local / d.tpr;
-    f(p, tr, (local - tr * d.tpr) * kTW);
+    return p;
   }
+
+  // Copy q (0 .. 17) of segment g: 0..8 plane rows, 9..11 mask rows, 12..14 the wrap blocks of
+  // column nx - 1 (planes 1, 5, 8; segment starting at x = 0), 15..17 those of column 0 (planes
+  // 3, 6, 7; segment ending at x = nx - 1). Returns its byte count (0: not needed) and issues it
+  // when `go`.
+  __device__ __forceinline__ uint32_t copy(const StepArgs<ST, Phys>& p, unsigned char* base, uint64_t* full,
+                                           const Segment& sg, int g, int q, bool go) const {
+    const int nx = p.g.nx, ny = p.g.ny, spr = (nx + S::SW - 1) / S::SW;
+    const int y = sg.y;
+    const int ym = y == 0 ? ny - 1 : y - 1;
+    const int yp = y == ny - 1 ? 0 : y + 1;
+    if (q < kQ) {
+      const int x0 = sg.j_lo * S::SW;
+      const int xs = x0 - S::H > 0 ? x0 - S::H : 0;
+      const int xe0 = (sg.j_hi + 1) * S::SW + S::H;
+      const int xe = xe0 < p.g.pitch ? xe0 : p.g.pitch;
+      const uint32_t bytes = static_cast<uint32_t>((xe - xs) * sizeof(ST));
+      if (go) {
+        ST* dst = reinterpret_cast<ST*>(base) + q * S::SROW + sg.w_first * S::SW + 2 * g * S::H + (xs - (x0 - S::H));
+        bulk_copy_g2s(dst, p.src + q * p.g.plane + static_cast<long long>(src_row(q, y, ym, yp)) * p.g.pitch + xs,
+                      bytes, full);
+      }
+      return bytes;
+    }
+    if (q < kQ + 3) {
+      const int r = q - kQ;
+      const int row = r == 0 ? ym : (r == 1 ? y : yp);
+      if (go) {
+        uint32_t* sm = reinterpret_cast<uint32_t*>(base + S::kPlaneBytes) + (g * 3 + r) * S::MW;
+        bulk_copy_g2s(sm, p.mask + static_cast<size_t>(row) * p.g.mask_words + (((sg.j_lo * S::SW) >> 5) & ~3),
+                      S::MW * 4, full);
+      }
+      return S::MW * 4;
+    }
+    const int wj = q - kQ - 3;  // wrap block 0..5
+    const bool lo = wj < 3;
+    if (lo ? sg.j_lo != 0 : sg.j_hi != spr - 1) return 0;
+    const int i = wrap_dir(wj);
+    if (go) {
+      ST* wr = reinterpret_cast<ST*>(base + S::kPlaneBytes + S::kMaskBytes) + (g * 6 + wj) * S::H;
+      const int xb = lo ? ((nx - 1) & ~(S::H - 1)) : 0;
+      bulk_copy_g2s(wr, p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xb, 16,
+                    full);
+    }
+    return 16;
+  }
+
+  // Producer (all 32 lanes): lane 0 arms the stage's barrier with the tile's byte count, then
+  // the lanes issue the tile's copies (18 per segment, those that apply) between them.
+  __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
+    const int k = instance_of(tile);
+    const Inst& d = a.inst[k];
+    const StepArgs<ST, Phys> p = grid_of(d);
+    const int strips = d.spr * d.g.ny;
+    const int s0 = (tile - s_tile0[k]) * kW;
+    const int s1 = s0 + kW < strips ? s0 + kW : strips;
+    const int ya = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s0)));
+    const int nseg = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s1 - 1))) - ya + 1;
+    uint32_t bytes = 0;
+    for (int c = lane; c < nseg * 18; c += 32) {
+      const int g = c / 18;
+      bytes += copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, false);
+    }
+    bytes = __reduce_add_sync(0xffffffffu, bytes);
+    if (lane == 0) mbar_arrive_expect_tx(full, bytes + kInstBytes);
+    __syncwarp();
+    if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, &d, kInstBytes, full);
+    for (int c = lane; c < nseg * 18; c += 32) {
+      const int g = c / 18;
+      copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, true);
+    }
+  }
+
+  __device__ __forceinline__ void consume(int tile, const unsigned char* base, int cw, int lane) const {
+    const Inst& d = *reinterpret_cast<const Inst*>(base + S::kStageBytes);
+    const int strips = d.spr * d.g.ny;
+    const int s0 = (tile - d.tile0) * kW;
+    const int s = s0 + cw;
+    if (s >= strips) return;
+    const StepArgs<ST, Phys> p = grid_of(d);
+    const int ya = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s0)));
+    const int y = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s)));
+    const int j = s - y * d.spr;
+    const int g = y - ya;
+    const int j_lo = g == 0 ? s0 - ya * d.spr : 0;
+    const int ny = p.g.ny;
+    const int ym = y == 0 ? ny - 1 : y - 1;
+    const int yp = y == ny - 1 ? 0 : y + 1;
+    const ST* st = reinterpret_cast<const ST*>(base);
+    const uint32_t* sm = reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes) + g * 3 * S::MW;
+    const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes) + g * 6 * S::H;
+    const int x0 = j * S::SW;
+    const int lx0 = cw * S::SW + (2 * g + 1) * S::H;
+    const int w0 = (x0 >> 5) - (((j_lo * S::SW) >> 5) & ~3);  // strip's first staged mask word
+    uint32_t mine = 0;
+    if (lane < 3 * (S::WPS + 1)) mine = sm[(lane / (S::WPS + 1)) * S::MW + w0 + lane % (S::WPS + 1)];
+    const bool solids = __any_sync(0xffffffffu, mine != 0u);
+#pragma unroll 1
+    for (int c = 0; c < kC; ++c) {
+      const int x = x0 + 32 * S::LC * c + S::LC * lane;
+      if (x < p.g.nx) {
+        const int lx = lx0 + 32 * S::LC * c + S::LC * lane;
+        if constexpr (S::LC == 2)
+          ring_pair<ST, false, S>(p, st, sm, wr, y, x, lx, w0 + 2 * c, lane, solids);
+        else
+          ring_cell<ST, typename Phys::Arith, false, S>(p, st, sm, wr, y, ym, yp, x, lx, w0 + c, lane, solids);
+      }
+    }
+  }
+
+  __device__ __forceinline__ void finish(int, int) const {}
 };
+
+// Shared memory of a batch ring block before the staged first-tile indices: the stages and the
+// ring's barriers.
+template <class Pol>
+__host__ __device__ constexpr size_t batch_ring_smem(int stages) {
+  return static_cast<size_t>(stages) * Pol::kStageBytes + 2 * stages * sizeof(uint64_t);
+}
 
 // Resident blocks per SM the register budget of a ring shape is capped for: 27 to 30 warps per SM
 // for the FP32 and 16-bit collisions (72 to 80 registers), none for FP64 (FP64-ALU-bound).
@@ -149,13 +323,13 @@ constexpr int batch_ring_min_blocks() {
 template <class ST, class Phys, int kW, int kC, int kStages>
 __global__ void __launch_bounds__(32 * (kW + 1), (batch_ring_min_blocks<ST, kW>()))
     batch_ring_kernel(const BatchArgs<ST, Phys> a, int tiles, int* err) {
-  using S = RingShape<ST, kW, kC>;
+  using Pol = BatchFlatPolicy<ST, Phys, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
-  int* s_tile0 = reinterpret_cast<int*>(smem + ring_smem_bytes<S>(kStages));
+  int* s_tile0 = reinterpret_cast<int*>(smem + batch_ring_smem<Pol>(kStages));
   for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_tile0[k] = a.inst[k].tile0;
   __syncthreads();
-  const BatchTiles<ST, Phys, S::TW> tiles_of{a, s_tile0};
-  ring_pipeline<ST, Phys, false, kW, kC, kStages>(smem, tiles_of, tiles, err);
+  Pol pol{a, s_tile0};
+  tile_pipeline<kW, kStages, Pol::kStageBytes>(smem, pol, tiles, err);
 }
 
 template <class ST>
@@ -216,7 +390,7 @@ struct lbm_batch {
   // ring kernel; tiles: the ring kernel's tile count
   int G = 0, block = kBatchThreads, grid = 0, items = 0, tiles = 0, grid_eff = 1;
   int ring_w = 8, ring_c = 2, ring_s = 2;  // ring tile shape: consumer warps, passes; stages
-  int table_tw = 0;            // ring tile width the table's tile indices were built for
+  int table_sw = 0, table_kw = 0;  // ring strip width and strips per tile of the table's tiles
   cudaStream_t stream = nullptr;
   cudaEvent_t ev[2] = {nullptr, nullptr};
   cudaGraphExec_t graph = nullptr;
@@ -264,11 +438,12 @@ int build_table(lbm_batch* b, int G) {
     d.g = in.g;
     d.cpr = (in.nx + 32 * G - 1) / (32 * G);
     d.item0 = item;
-    d.tpr = (in.nx + b->table_tw - 1) / b->table_tw;
+    d.spr = (in.nx + b->table_sw - 1) / b->table_sw;
+    d.spr_div = FastDiv(static_cast<uint32_t>(d.spr));
     d.tile0 = tile;
     d.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
     item += d.cpr * in.ny;
-    tile += d.tpr * in.ny;
+    tile += static_cast<int>((static_cast<long long>(d.spr) * in.ny + b->table_kw - 1) / b->table_kw);
   }
   b->tiles = tile;
   if (!b->table_d) B_CUDA(b, cudaMalloc(&b->table_d, b->count * sizeof(BatchInst<Consts>)));
@@ -285,7 +460,10 @@ int launch_batch_t(lbm_batch* b, int steps, bool prepare_only) {
   if (prepare_only) {
     // Everything that is not a stream operation happens here, outside any graph capture.
     if (b->table_G != G) {
-      if (b->table_tw == 0) b->table_tw = RingShape<ST, 8, 2>::TW;
+      if (b->table_sw == 0) {
+        b->table_sw = RingShape<ST, 8, 2>::SW;
+        b->table_kw = 8;
+      }
       if (int rc = build_table<ST>(b, G)) return rc;
     }
     int grid = b->grid;
@@ -322,12 +500,14 @@ int launch_batch_t(lbm_batch* b, int steps, bool prepare_only) {
 template <class ST, int kW, int kC, int kStages>
 int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
   using Phys = typename BForm<ST>::Phys;
-  using S = RingShape<ST, kW, kC>;
+  using S = FlatShape<ST, kW, kC>;
   const auto kernel = batch_ring_kernel<ST, Phys, kW, kC, kStages>;
-  const size_t smem = ring_smem_bytes<S>(kStages) + static_cast<size_t>(b->count) * sizeof(int);
+  const size_t smem = batch_ring_smem<BatchFlatPolicy<ST, Phys, kW, kC>>(kStages) +
+                      static_cast<size_t>(b->count) * sizeof(int);
   if (prepare_only) {
-    if (b->table_G == 0 || b->table_tw != S::TW) {
-      b->table_tw = S::TW;
+    if (b->table_G == 0 || b->table_sw != S::SW || b->table_kw != kW) {
+      b->table_sw = S::SW;
+      b->table_kw = kW;
       if (int rc = build_table<ST>(b, b->table_G ? b->table_G : StoreTraits<ST>::kVec)) return rc;
     }
     B_CUDA(b, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));

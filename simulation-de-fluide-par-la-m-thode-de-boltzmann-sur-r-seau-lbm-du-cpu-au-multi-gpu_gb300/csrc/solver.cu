@@ -219,7 +219,8 @@ int launch_ring_t(lbm_solver* s, int steps) {
       a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
       a.step_ctr = s->step_ctr;
       a.step_off = static_cast<uint32_t>(k);
-      kernel<<<grid, S::kThreads, smem, s->stream>>>(a, tpr, tiles, 0, s->err_flag);
+      LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, s->stream, a, tpr, tiles, 0,
+                                   s->err_flag));
       s->cur ^= 1;
     }
     LBM_CUDA(s, cudaGetLastError());
@@ -260,6 +261,8 @@ int launch_steps_o(lbm_solver* s, int steps) {
     case 15: return launch_ring_t<ST, kOpen, 4, 2, 3, 1>(s, steps);
     case 16: return launch_ring_t<ST, kOpen, 4, 2, 3, 7>(s, steps);
     case 17: return launch_ring_t<ST, kOpen, 8, 2, 2, 3>(s, steps);
+    case 18: return launch_ring_t<ST, kOpen, 8, 2, 3, 3>(s, steps);
+    case 19: return launch_ring_t<ST, kOpen, 8, 1, 4, 3>(s, steps);
     default: return launch_steps_t<ST, kOpen, 0>(s, steps);
   }
 }
@@ -852,7 +855,7 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
 
 int lbm_set_variant(lbm_solver* s, int variant) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
-  if (variant < -1 || variant > 17)
+  if (variant < -1 || variant > 19)
     return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 17]");
   s->variant = variant;
   lbm_b200::drop_step_graph(s);

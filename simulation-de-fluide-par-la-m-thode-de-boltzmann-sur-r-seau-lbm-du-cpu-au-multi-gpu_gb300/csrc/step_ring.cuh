@@ -25,6 +25,9 @@
 //     rows of a strip between its two ghost rows).
 #pragma once
 
+#include <type_traits>
+#include <utility>
+
 #include "step_tma.cuh"
 
 namespace lbm_b200 {
@@ -303,9 +306,17 @@ __device__ __forceinline__ void ring_consume_tile(const StepArgs<ST, Phys>& p, c
   }
 }
 
+// Policies whose producer issues its copies from all 32 lanes set kWarpIssue (pol.issue then
+// also gets the lane and must arm the barrier from one lane before any lane issues a copy).
+template <class P, class = void>
+struct warp_issue : std::false_type {};
+template <class P>
+struct warp_issue<P, std::void_t<decltype(P::kWarpIssue)>> : std::bool_constant<P::kWarpIssue> {};
+
 // Warp-specialised pipeline over tiles 0 .. tiles - 1 (grid-stride) with a ring of kStages
-// stages of kStageBytes: warp 0 (one lane) calls pol.issue(tile, stage, full_barrier), which
-// arms the barrier with its byte count and issues the bulk copies; consumer warps 1 .. kW wait
+// stages of kStageBytes: warp 0 (one lane, or all lanes for kWarpIssue policies) calls
+// pol.issue(tile, stage, full_barrier), which arms the barrier with its byte count and issues
+// the bulk copies; consumer warps 1 .. kW wait
 // for the stage, call pol.consume(tile, stage, consumer_warp, lane) and release it. Waits are
 // bounded (error flag). Afterwards every consumer warp (not the producer) calls
 // pol.finish(cw, lane), also after a wait ran out (the host then reports the timeout), e.g. to
@@ -326,23 +337,31 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
   __syncthreads();
 
   if (warp == 0) {
-    if (lane != 0) return;
+    constexpr bool kWarp = warp_issue<Pol>::value;
+    if (!kWarp && lane != 0) return;
     // Producer.
     int s = 0, issued = 0;
     uint32_t phase = 0;
     bool ok = true;
     for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++issued) {
-      if (issued >= kStages && !mbar_wait_bounded(&empty[s], phase ^ 1u, err)) {
-        ok = false;
-        break;
+      if (issued >= kStages) {
+        const bool got = kWarp ? mbar_wait_bounded_warp(&empty[s], phase ^ 1u, err)
+                               : mbar_wait_bounded(&empty[s], phase ^ 1u, err);
+        if (!got) {
+          ok = false;
+          break;
+        }
       }
-      pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s]);
+      if constexpr (kWarp)
+        pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s], lane);
+      else
+        pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s]);
       if (++s == kStages) {
         s = 0;
         phase ^= 1u;
       }
     }
-    if (!ok) {
+    if (!ok && lane == 0) {
       for (int k = 0; k < kStages && k < issued; ++k) {
         const int st = (s + kStages - 1 - k) % kStages;
         const int use = (issued - 1 - k) / kStages;
@@ -409,11 +428,39 @@ struct GridTiles {
   }
 };
 
+// Programmatic dependent launch, device side: wait until the previous kernel on the stream has
+// completed and its writes are visible (a no-op for a kernel launched without the attribute),
+// then let the next kernel's blocks be scheduled as this one's exit.
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Host side: a launch with programmatic stream serialisation, so that its blocks may be
+// scheduled while the previous kernel on the stream drains (they start with
+// grid_dependency_wait before touching memory).
+template <class... Params, class... Args>
+cudaError_t launch_dependent(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                             Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
     ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int row0, int* err) {
   using S = RingShape<ST, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
   const GridTiles<ST, Phys, S::TW> grid_tiles{p, tiles_per_row, row0};
   ring_pipeline<ST, Phys, kOpen, kW, kC, kStages>(smem, grid_tiles, tiles, err);
 }

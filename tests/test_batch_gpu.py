@@ -118,3 +118,48 @@ def test_ring_tile_shapes_equal_separate_launches(gpu_lib, orc, specs, shape, pr
         b.run_separate(70)
         for k in range(len(sub)):
             assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k}"
+
+
+def _odd_specs(gpu_lib):
+    """Instances narrower than one strip (a tile spans up to 8 rows), widths just off the strip
+    and tile widths (tiles straddle two rows), a few solid cells next to the periodic x edges."""
+    widths = [3, 5, 17, 31, 33, 63, 64, 65, 129, 200, 300, 513, 700, 1030]
+    heights = [5, 9, 6, 12, 40, 7, 33, 11, 20, 8, 13, 6, 9, 5]
+    rng = np.random.default_rng(5)
+    out = []
+    for k, (nx, ny) in enumerate(zip(widths, heights)):
+        mask = gpu_lib.make_channel(nx, ny).reshape(ny, nx).copy()
+        if ny > 4:
+            mask[ny // 2, 0] = 1
+            mask[ny // 2 + 1, nx - 1] = 1
+            mask[1 + rng.integers(ny - 2), rng.integers(nx)] = 1
+        out.append({"nx": nx, "ny": ny, "mask": mask.reshape(-1).astype(np.uint8),
+                    "tau": 0.55 + 0.03 * k, "fx": 2e-6 * (1 + k % 3), "fy": 0.0, "seed": 900 + k})
+    return out
+
+
+@pytest.mark.parametrize("shape", [(8, 2, 2), (4, 2, 4), (4, 1, 4), (2, 2, 2)])
+@pytest.mark.parametrize("precision", ["fp32", "fp16"])
+def test_odd_widths_multi_row_tiles(gpu_lib, orc, shape, precision):
+    sub = _odd_specs(gpu_lib)
+    real = "f32"
+    with gpu_lib.Batch(sub, precision=precision) as a, gpu_lib.Batch(sub, precision=precision) as b:
+        _fill(a, sub, orc, real)
+        _fill(b, sub, orc, real)
+        a.set_tiles(*shape)
+        a.run(70)
+        b.run_separate(70)
+        for k in range(len(sub)):
+            assert np.array_equal(a.populations(k), b.populations(k)), f"instance {k} ({sub[k]['nx']}x{sub[k]['ny']})"
+
+
+def test_odd_widths_bit_exact(gpu_lib, orc):
+    sub = _odd_specs(gpu_lib)
+    with gpu_lib.Batch(sub, precision="fp32") as b:
+        _fill(b, sub, orc)
+        b.run(60)
+        for k, s in enumerate(sub):
+            nx, ny, m = s["nx"], s["ny"], s["mask"]
+            r = orc.s_to_r(nx, ny, m, orc.seeded_state(s["seed"], 1e-4, nx, ny, m))
+            orc.pull_run(nx, ny, m, float(np.float32(s["tau"])), s["fx"], 0.0, r, 60)
+            assert np.array_equal(b.populations(k), orc.r_to_s(nx, ny, m, r)), f"instance {k} ({nx}x{ny})"
