@@ -51,8 +51,17 @@ struct alignas(16) BatchInst {
   int item0;   // first global chunk index
   int spr;     // ring strips per row (strips of the tile shape's strip width)
   FastDiv spr_div;
+  int rpt;     // ring tiles of whole rows: rows per tile (0: tiles of consecutive strips)
   int tile0;   // first global ring tile index
   Consts k;
+};
+
+// The step arguments of one instance for one buffer parity (source buffer 0 or 1), built on the
+// host with the table; 16-byte aligned and sized so that the ring kernel's producer can copy a
+// tile's entry into the tile's stage.
+template <class ST, class Phys>
+struct alignas(16) StagedArgs {
+  StepArgs<ST, Phys> p;
 };
 
 template <class ST, class Phys>
@@ -65,6 +74,8 @@ struct BatchArgs {
   int items;
   PlaneScales sc;
   const uint32_t* step;  // lattice steps taken (device counter; stochastic-rounding key)
+  const StagedArgs<ST, Phys>* args;  // [instance][parity]
+  int parity;                        // src == buffer `parity`
 };
 
 // Device step counter of a batch: read by every step launch, advanced by one after it (inside a
@@ -153,18 +164,30 @@ __device__ __forceinline__ Segment tile_segment(int g, int s0, int s1, int ya, i
   return sg;
 }
 
-// Stage of the batch ring: the tile's rows, masks and wrap blocks (FlatShape), then the table
-// entry of the tile's instance, copied by the producer with the rest, so that the consumers
-// neither search the table nor wait on global loads of it.
+// Where consumer warp w's strip lies: its row (and the rows above and below), first cell, first
+// stage element, first staged mask word, offsets of its 3 staged mask rows (words) and of its
+// wrap blocks (elements), flags (kStripValid: the warp has a strip; kStripRows: the stage holds
+// whole rows, periodic neighbours come from the row itself).
+constexpr int kStripValid = 1, kStripRows = 2;
+struct alignas(16) StripDesc {
+  int y, ym, yp, x0, lx0, w0, sm_off, wr_off, flags;
+};
+
+// Stage of the batch ring: the tile's rows, masks and wrap blocks (FlatShape), then the step
+// arguments of the tile's instance (copied by the producer with the rest) and the kW strip
+// descriptors (written by the producer's lanes before it arms the barrier), so that the
+// consumers neither search the table, nor hold the instance's constants in registers, nor repeat
+// the strip arithmetic in every warp.
 template <class ST, class Phys, int kW, int kC>
 struct BatchFlatPolicy {
   using S = FlatShape<ST, kW, kC>;
   using Inst = BatchInst<typename Phys::Consts>;
   static constexpr bool kFinish = false;
   static constexpr bool kWarpIssue = true;
-  static constexpr int kInstBytes = static_cast<int>(sizeof(Inst));
-  static constexpr int kStageBytes = S::kStageBytes + kInstBytes;
-  static_assert(kInstBytes % 16 == 0, "table entries are copied in 16-byte units");
+  static constexpr int kArgsBytes = static_cast<int>(sizeof(StagedArgs<ST, Phys>));
+  static constexpr int kDescOff = S::kStageBytes + kArgsBytes;
+  static constexpr int kStageBytes = kDescOff + kW * static_cast<int>(sizeof(StripDesc));
+  static_assert(kArgsBytes % 16 == 0, "step arguments are copied in 16-byte units");
   const BatchArgs<ST, Phys>& a;
   const int* s_tile0;
 
@@ -240,67 +263,145 @@ struct BatchFlatPolicy {
     return 16;
   }
 
-  // Producer (all 32 lanes): lane 0 arms the stage's barrier with the tile's byte count, then
-  // the lanes issue the tile's copies (18 per segment, those that apply) between them.
+  // Copy c of a whole-row tile (rows ya .. ya + rn - 1): c < 18 plane i = c / 2 rows ya - c_y ..,
+  // split where they wrap past row ny - 1 (run c % 2), one copy per run into plane i's stage rows
+  // at pitch stride; 18 .. 18 + rn + 1: mask row ya - 1 + (c - 18), words 0 .. MW - 1.
+  __device__ __forceinline__ uint32_t row_copy(const StepArgs<ST, Phys>& p, unsigned char* base, uint64_t* full,
+                                               int ya, int rn, int c, bool go) const {
+    const int ny = p.g.ny, pitch = p.g.pitch;
+    if (c < 2 * kQ) {
+      const int i = c >> 1;
+      int r0 = ya - dir_cy(i);
+      r0 = r0 < 0 ? r0 + ny : (r0 >= ny ? r0 - ny : r0);
+      const int len0 = rn < ny - r0 ? rn : ny - r0;
+      const int rs = (c & 1) ? 0 : r0;
+      const int len = (c & 1) ? rn - len0 : len0;
+      if (len <= 0) return 0;
+      const uint32_t bytes = static_cast<uint32_t>(len) * pitch * sizeof(ST);
+      if (go)
+        bulk_copy_g2s(reinterpret_cast<ST*>(base) + i * S::SROW + ((c & 1) ? len0 : 0) * pitch,
+                      p.src + i * p.g.plane + static_cast<long long>(rs) * pitch, bytes, full);
+      return bytes;
+    }
+    const int k = c - 2 * kQ;
+    if (k >= rn + 2) return 0;
+    int m = ya - 1 + k;
+    m = m < 0 ? m + ny : (m >= ny ? m - ny : m);
+    if (go)
+      bulk_copy_g2s(reinterpret_cast<uint32_t*>(base + S::kPlaneBytes) + k * S::MW,
+                    p.mask + static_cast<size_t>(m) * p.g.mask_words, S::MW * 4, full);
+    return S::MW * 4;
+  }
+
+  // Producer (all 32 lanes): the lanes describe the consumer warps' strips and size the tile's
+  // copies; lane 0 arms the stage's barrier with the byte count; then the lanes issue the copies
+  // between them (strip tiles: 18 per segment, those that apply; whole-row tiles: at most
+  // 2 per plane and one per mask row) and lane 0 the step arguments' copy.
   __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
     const int k = instance_of(tile);
     const Inst& d = a.inst[k];
     const StepArgs<ST, Phys> p = grid_of(d);
-    const int strips = d.spr * d.g.ny;
+    const int ny = d.g.ny;
+    uint32_t bytes = 0;
+    StripDesc sd;
+    if (d.rpt) {
+      const int ya = (tile - s_tile0[k]) * d.rpt;
+      const int rn = d.rpt < ny - ya ? d.rpt : ny - ya;
+      if (lane < 2 * kQ + rn + 2) bytes = row_copy(p, base, full, ya, rn, lane, false);
+      const int r = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(lane)));
+      const int j = lane - r * d.spr;
+      sd.flags = (r < rn ? kStripValid : 0) | kStripRows;
+      sd.y = r < rn ? ya + r : ya;
+      sd.x0 = j * S::SW;
+      sd.lx0 = r * d.g.pitch + sd.x0;
+      sd.w0 = sd.x0 >> 5;
+      sd.sm_off = r * S::MW;
+      sd.wr_off = 0;
+      bytes = __reduce_add_sync(0xffffffffu, bytes);
+      if (lane < kW) {
+        sd.ym = sd.y == 0 ? ny - 1 : sd.y - 1;
+        sd.yp = sd.y == ny - 1 ? 0 : sd.y + 1;
+        reinterpret_cast<StripDesc*>(base + kDescOff)[lane] = sd;
+      }
+      __syncwarp();
+      if (lane == 0) {
+        mbar_arrive_expect_tx(full, bytes + kArgsBytes);
+        bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
+      }
+      __syncwarp();
+      if (lane < 2 * kQ + rn + 2) row_copy(p, base, full, ya, rn, lane, true);
+      return;
+    }
+    const int strips = d.spr * ny;
     const int s0 = (tile - s_tile0[k]) * kW;
     const int s1 = s0 + kW < strips ? s0 + kW : strips;
     const int ya = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s0)));
     const int nseg = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s1 - 1))) - ya + 1;
-    uint32_t bytes = 0;
     for (int c = lane; c < nseg * 18; c += 32) {
       const int g = c / 18;
       bytes += copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, false);
     }
     bytes = __reduce_add_sync(0xffffffffu, bytes);
-    if (lane == 0) mbar_arrive_expect_tx(full, bytes + kInstBytes);
+    if (lane < kW) {
+      // Lane w describes consumer warp w's strip (ordered before lane 0's arrive by __syncwarp;
+      // the consumers acquire it with the barrier phase).
+      const int st = s0 + lane;
+      const bool valid = st < s1;
+      sd.flags = valid ? kStripValid : 0;
+      sd.y = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(valid ? st : s0)));
+      const int j = (valid ? st : s0) - sd.y * d.spr;
+      const int g = sd.y - ya;
+      const int j_lo = g == 0 ? s0 - ya * d.spr : 0;
+      sd.ym = sd.y == 0 ? ny - 1 : sd.y - 1;
+      sd.yp = sd.y == ny - 1 ? 0 : sd.y + 1;
+      sd.x0 = j * S::SW;
+      sd.lx0 = lane * S::SW + (2 * g + 1) * S::H;
+      sd.w0 = (sd.x0 >> 5) - (((j_lo * S::SW) >> 5) & ~3);
+      sd.sm_off = g * 3 * S::MW;
+      sd.wr_off = g * 6 * S::H;
+      reinterpret_cast<StripDesc*>(base + kDescOff)[lane] = sd;
+    }
     __syncwarp();
-    if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, &d, kInstBytes, full);
+    if (lane == 0) mbar_arrive_expect_tx(full, bytes + kArgsBytes);
+    __syncwarp();
+    if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
     for (int c = lane; c < nseg * 18; c += 32) {
       const int g = c / 18;
       copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, true);
     }
   }
 
-  __device__ __forceinline__ void consume(int tile, const unsigned char* base, int cw, int lane) const {
-    const Inst& d = *reinterpret_cast<const Inst*>(base + S::kStageBytes);
-    const int strips = d.spr * d.g.ny;
-    const int s0 = (tile - d.tile0) * kW;
-    const int s = s0 + cw;
-    if (s >= strips) return;
-    const StepArgs<ST, Phys> p = grid_of(d);
-    const int ya = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s0)));
-    const int y = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s)));
-    const int j = s - y * d.spr;
-    const int g = y - ya;
-    const int j_lo = g == 0 ? s0 - ya * d.spr : 0;
-    const int ny = p.g.ny;
-    const int ym = y == 0 ? ny - 1 : y - 1;
-    const int yp = y == ny - 1 ? 0 : y + 1;
+  template <bool kRows>
+  __device__ __forceinline__ void strip(const StepArgs<ST, Phys>& p, const StripDesc& sd, const unsigned char* base,
+                                        int lane) const {
     const ST* st = reinterpret_cast<const ST*>(base);
-    const uint32_t* sm = reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes) + g * 3 * S::MW;
-    const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes) + g * 6 * S::H;
-    const int x0 = j * S::SW;
-    const int lx0 = cw * S::SW + (2 * g + 1) * S::H;
-    const int w0 = (x0 >> 5) - (((j_lo * S::SW) >> 5) & ~3);  // strip's first staged mask word
+    const uint32_t* sm = reinterpret_cast<const uint32_t*>(base + S::kPlaneBytes) + sd.sm_off;
+    const ST* wr = reinterpret_cast<const ST*>(base + S::kPlaneBytes + S::kMaskBytes) + sd.wr_off;
     uint32_t mine = 0;
-    if (lane < 3 * (S::WPS + 1)) mine = sm[(lane / (S::WPS + 1)) * S::MW + w0 + lane % (S::WPS + 1)];
+    if (lane < 3 * (S::WPS + 1)) mine = sm[(lane / (S::WPS + 1)) * S::MW + sd.w0 + lane % (S::WPS + 1)];
     const bool solids = __any_sync(0xffffffffu, mine != 0u);
 #pragma unroll 1
     for (int c = 0; c < kC; ++c) {
-      const int x = x0 + 32 * S::LC * c + S::LC * lane;
+      const int x = sd.x0 + 32 * S::LC * c + S::LC * lane;
       if (x < p.g.nx) {
-        const int lx = lx0 + 32 * S::LC * c + S::LC * lane;
+        const int lx = sd.lx0 + 32 * S::LC * c + S::LC * lane;
         if constexpr (S::LC == 2)
-          ring_pair<ST, false, S>(p, st, sm, wr, y, x, lx, w0 + 2 * c, lane, solids);
+          ring_pair<ST, false, S, kRows>(p, st, sm, wr, sd.y, x, lx, sd.w0 + 2 * c, lane, solids);
         else
-          ring_cell<ST, typename Phys::Arith, false, S>(p, st, sm, wr, y, ym, yp, x, lx, w0 + c, lane, solids);
+          ring_cell<ST, typename Phys::Arith, false, S, kRows>(p, st, sm, wr, sd.y, sd.ym, sd.yp, x, lx,
+                                                               sd.w0 + c, lane, solids);
       }
     }
+  }
+
+  __device__ __forceinline__ void consume(int, const unsigned char* base, int cw, int lane) const {
+    const StripDesc sd = reinterpret_cast<const StripDesc*>(base + kDescOff)[cw];
+    if (!(sd.flags & kStripValid)) return;
+    const StepArgs<ST, Phys>& p = reinterpret_cast<const StagedArgs<ST, Phys>*>(base + S::kStageBytes)->p;
+    if (sd.flags & kStripRows)
+      strip<true>(p, sd, base, lane);
+    else
+      strip<false>(p, sd, base, lane);
   }
 
   __device__ __forceinline__ void finish(int, int) const {}
@@ -379,6 +480,7 @@ struct lbm_batch {
   int cur = 0;
   uint32_t* mask_d = nullptr;
   void* table_d = nullptr;  // BatchInst<Consts>[count] for the current G
+  void* args_d = nullptr;   // StagedArgs[count][2] (step arguments per instance and parity)
   int table_G = 0;
   void* stage = nullptr;
   size_t stage_bytes = 0;
@@ -440,12 +542,35 @@ int build_table(lbm_batch* b, int G) {
     d.item0 = item;
     d.spr = (in.nx + b->table_sw - 1) / b->table_sw;
     d.spr_div = FastDiv(static_cast<uint32_t>(d.spr));
+    // Whole-row tiles for instances of at most half a tile per row (few copies per tile);
+    // tiles of consecutive strips otherwise (no idle warps).
+    d.rpt = 2 * d.spr <= b->table_kw ? b->table_kw / d.spr : 0;
     d.tile0 = tile;
     d.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
     item += d.cpr * in.ny;
-    tile += static_cast<int>((static_cast<long long>(d.spr) * in.ny + b->table_kw - 1) / b->table_kw);
+    tile += d.rpt ? (in.ny + d.rpt - 1) / d.rpt
+                  : static_cast<int>((static_cast<long long>(d.spr) * in.ny + b->table_kw - 1) / b->table_kw);
   }
   b->tiles = tile;
+  using Phys = typename BForm<ST>::Phys;
+  std::vector<StagedArgs<ST, Phys>> args(2 * static_cast<size_t>(b->count));
+  for (int k = 0; k < b->count; ++k) {
+    for (int par = 0; par < 2; ++par) {
+      StepArgs<ST, Phys>& p = args[2 * k + par].p;
+      p = StepArgs<ST, Phys>{};
+      p.src = static_cast<const ST*>(b->buf[par]) + tab[k].off;
+      p.dst = static_cast<ST*>(b->buf[par ^ 1]) + tab[k].off;
+      p.mask = b->mask_d + tab[k].mask_off;
+      p.g = tab[k].g;
+      p.k = tab[k].k;
+      p.sc = b->sc;
+      p.step_ctr = b->step_d;
+      p.step_off = 0;
+      p.key_base = tab[k].off / kQ;
+    }
+  }
+  if (!b->args_d) B_CUDA(b, cudaMalloc(&b->args_d, args.size() * sizeof(args[0])));
+  B_CUDA(b, cudaMemcpy(b->args_d, args.data(), args.size() * sizeof(args[0]), cudaMemcpyHostToDevice));
   if (!b->table_d) B_CUDA(b, cudaMalloc(&b->table_d, b->count * sizeof(BatchInst<Consts>)));
   B_CUDA(b, cudaMemcpy(b->table_d, tab.data(), b->count * sizeof(BatchInst<Consts>), cudaMemcpyHostToDevice));
   b->items = item;
@@ -527,10 +652,12 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
   a.items = b->items;
   a.sc = b->sc;
   a.step = b->step_d;
+  a.args = static_cast<const StagedArgs<ST, Phys>*>(b->args_d);
   int* err = reinterpret_cast<int*>(b->step_d + 1);
   for (int s = 0; s < steps; ++s) {
     a.src = static_cast<const ST*>(b->buf[b->cur]);
     a.dst = static_cast<ST*>(b->buf[b->cur ^ 1]);
+    a.parity = b->cur;
     kernel<<<b->grid_eff, S::kThreads, smem, b->stream>>>(a, b->tiles, err);
     step_counter_add<<<1, 1, 0, b->stream>>>(b->step_d);
     ++b->t;
@@ -867,7 +994,7 @@ int lbm_batch_destroy(lbm_batch* b) {
   if (!b) return LBM_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->stage,
+  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->args_d, b->stage,
                   static_cast<void*>(b->red), static_cast<void*>(b->step_d)})
     cudaFree(p);
   for (cudaEvent_t ev : b->ev)

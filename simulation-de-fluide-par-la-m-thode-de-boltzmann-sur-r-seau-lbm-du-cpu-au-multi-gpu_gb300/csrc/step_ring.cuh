@@ -63,7 +63,9 @@ __device__ __forceinline__ int wrap_dir(int j) {
 
 // One cell of a strip. st: stage planes (plane i row at st + i * SROW, local column lx = cell x);
 // sm: 3 staged mask rows (y - 1, y, y + 1) whose word 0 is word tx0 / 32; wr: wrap blocks.
-template <class ST, class A, bool kOpen, class S>
+// kWrapInRow: the stage holds the cell's whole row (columns 0 .. nx - 1 at lx - x ..), and the
+// periodic neighbours of x = 0 and x = nx - 1 are read from it instead of from wrap blocks.
+template <class ST, class A, bool kOpen, class S, bool kWrapInRow = false>
 __device__ __forceinline__ void ring_cell(const StepArgs<ST, ExactPhys<A>>& p, const ST* st,
                                           const uint32_t* sm, const ST* wr, int y, int ym, int yp,
                                           int x, int lx, int word, int lane, bool solids) {
@@ -73,7 +75,19 @@ __device__ __forceinline__ void ring_cell(const StepArgs<ST, ExactPhys<A>>& p, c
   T v[kQ];
 #pragma unroll
   for (int i = 0; i < kQ; ++i) v[i] = st[i * S::SROW + lx - dir_cx(i)];
-  if (!kOpen) {
+  if (!kOpen && kWrapInRow) {
+    const int r0 = lx - x;  // column 0 of the staged row
+    if (x == 0) {
+      v[1] = st[1 * S::SROW + r0 + nx - 1];
+      v[5] = st[5 * S::SROW + r0 + nx - 1];
+      v[8] = st[8 * S::SROW + r0 + nx - 1];
+    }
+    if (x == nx - 1) {
+      v[3] = st[3 * S::SROW + r0];
+      v[6] = st[6 * S::SROW + r0];
+      v[7] = st[7 * S::SROW + r0];
+    }
+  } else if (!kOpen) {
     if (x == 0) {
       const int k = (nx - 1) & (S::H - 1);
       v[1] = wr[0 * S::H + k];
@@ -146,8 +160,9 @@ __device__ __forceinline__ float2 widen_pair<__nv_bfloat16>(uint32_t raw) {
 }
 
 // One pair of cells x, x + 1 (x even) of a strip, 16-bit storage, FP32 fast collision. Same
-// stage layout as ring_cell; word / lane locate the pair's mask bits (cells x - 1 .. x + 2).
-template <class ST, bool kOpen, class S>
+// stage layout (and kWrapInRow) as ring_cell; word / lane locate the pair's mask bits (cells
+// x - 1 .. x + 2).
+template <class ST, bool kOpen, class S, bool kWrapInRow = false>
 __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const ST* st,
                                           const uint32_t* sm, const ST* wr, int y, int x, int lx,
                                           int word, int lane, bool solids) {
@@ -164,7 +179,24 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
     if (dir_cx(i) == -1) raw = __byte_perm(own, r[1], 0x5432);   // cells x + 1, x + 2
     v[i] = widen_pair<ST>(raw);
   }
-  if (!kOpen) {
+  if (!kOpen && kWrapInRow) {
+    const int r0 = lx - x;  // column 0 of the staged row
+    if (x == 0) {
+      v[1].x = widen<ST>(st[1 * S::SROW + r0 + nx - 1]);
+      v[5].x = widen<ST>(st[5 * S::SROW + r0 + nx - 1]);
+      v[8].x = widen<ST>(st[8 * S::SROW + r0 + nx - 1]);
+    }
+    if (x == nx - 1) {
+      v[3].x = widen<ST>(st[3 * S::SROW + r0]);
+      v[6].x = widen<ST>(st[6 * S::SROW + r0]);
+      v[7].x = widen<ST>(st[7 * S::SROW + r0]);
+    }
+    if (x + 1 == nx - 1) {
+      v[3].y = widen<ST>(st[3 * S::SROW + r0]);
+      v[6].y = widen<ST>(st[6 * S::SROW + r0]);
+      v[7].y = widen<ST>(st[7 * S::SROW + r0]);
+    }
+  } else if (!kOpen) {
     if (x == 0) {
       const int k = (nx - 1) & (S::H - 1);
       v[1].x = widen<ST>(wr[0 * S::H + k]);
