@@ -20,6 +20,7 @@ included (reference src/common/driver.hpp:120).
             the 16-bit forms' velocity error and mass drift against FP64 (cylinder wake);
             the adjoint's forward and backward step times (512 x 128 channel, batch of 32);
             the batched ensemble (256 uneven channels) against one launch per instance;
+            the plain method at every at-scale grid (2048^2, 4096^2, 8192^2; FP32 and FP64);
             the cylinder wake at Re 100 in every form (Strouhal number, lift, drag).
   cpu_baseline  the oracle's OpenMP port of the reference's v1 solver on the host cores.
 
@@ -168,11 +169,14 @@ def max_over_ranks(x: float, dist) -> float:
     return float(t.item())
 
 
-def channel_state(orc, n: int, precision_real: str):
+def channel_state(n: int, precision_real: str):
+    """The at-scale workload's walled channel and its seeded perturbation (the package's
+    synthetic-input generator; the oracle is not used outside the CPU-baseline leg)."""
     import __graft_entry__ as entry
     pkg = entry.package()
     mask = pkg.make_channel(n, n)
-    s0 = orc.seeded_state(SEED, AMP, n, n, mask, precision_real)
+    dtype = np.float64 if precision_real == "f64" else np.float32
+    s0 = pkg.workloads.seeded_state(SEED, AMP, n, n, mask, dtype)
     return pkg, mask, s0
 
 
@@ -221,6 +225,28 @@ def accuracy_report(pkg):
                      if k != "form"}
     out["workload"] = (f"cylinder wake {nx}x{ny}, disc D=32 at (256,129), tau {tau}, "
                        f"F=({fx},0), start u=(0.05,0), {steps} steps, stochastic rounding")
+    return out
+
+
+def scale_report(pkg, peak):
+    """The plain method at every grid of the at-scale workload (walled channel, tau 0.6,
+    F = (1e-6, 0), seeded perturbation in [-1e-4, 1e-4]): 2048^2, 4096^2, 8192^2 in FP32
+    (1000 steps each) and FP64 (1000, 1000 and 200 steps: FP64-ALU-bound, 25 ms per step at
+    8192^2), device-resident MLUPS and the fraction of the 72 / 144 B per cell roofline."""
+    out = {}
+    for prec, real, steps in (("fp32", "f32", (1000, 1000, 1000)), ("fp64", "f64", (1000, 1000, 200))):
+        out[prec] = {}
+        for n, k in zip((2048, 4096, 8192), steps):
+            try:
+                mask = pkg.make_channel(n, n)
+                s0 = pkg.workloads.seeded_state(SEED, AMP, n, n, mask, np.float64 if real == "f64" else np.float32)
+                ml, _ = time_form(pkg, mask, s0, n, prec, k, 10)
+                del s0
+                gbs = BYTES_PER_CELL[prec] * ml * 1e6 / 1e9
+                out[prec][str(n)] = {"mlups": round(ml, 1), "achieved_gbs": round(gbs, 1),
+                                     "hbm_frac": round(gbs / peak, 4), "steps": k}
+            except Exception as e:
+                out[prec][str(n)] = {"error": str(e)[:200]}
     return out
 
 
@@ -312,13 +338,10 @@ def run_ours(args):
     torch.cuda.set_device(local)
     pkg = entry.package()
     pkg.build()
-    orc = entry.oracle_module()
-    if not orc.LIB.exists():
-        orc.build()
     n = args.nx
     warmup = max(args.warmup, 3)
     prec = args.precision
-    _, mask, s0 = channel_state(orc, n, "f32")
+    _, mask, s0 = channel_state(n, "f32")
     s_head = s0.astype(np.float64) if prec == "fp64" else s0
 
     solver = pkg.Solver(n, n, TAU, FX, FY, mask, precision=prec)
@@ -401,11 +424,16 @@ def run_ours(args):
             forms["adjoint"] = adjoint_report(pkg, peak)
         if args.batch:
             forms["batch"] = batch_report(pkg, peak)
+        if args.scale:
+            forms["scale"] = scale_report(pkg, peak)
         if args.wake:
             forms["cylinder_wake"] = wake_report(pkg)
 
     cpu = None
     if rank == 0 and args.cpu_baseline:
+        orc = entry.oracle_module()  # the CPU-baseline leg is the oracle's one use here
+        if not orc.LIB.exists():
+            orc.build()
         cpu = cpu_baseline(orc, n)
 
     if rank != 0:
@@ -514,6 +542,8 @@ def main():
                     help="skip the adjoint form")
     ap.add_argument("--no-batch", dest="batch", action="store_false",
                     help="skip the batched ensemble form")
+    ap.add_argument("--no-scale", dest="scale", action="store_false",
+                    help="skip the 2048^2 / 4096^2 / 8192^2 FP32 and FP64 scale report")
     ap.add_argument("--no-wake", dest="wake", action="store_false",
                     help="skip the cylinder-wake comparison of the forms")
     args = ap.parse_args()

@@ -26,9 +26,14 @@ def uniform01(seed: int, count: int, offset: int = 0) -> np.ndarray:
 
 
 def seeded_state(seed: int, amp: float, nx: int, ny: int, solid, dtype=np.float32) -> np.ndarray:
-    """f_i - w_i = U(-amp, amp) per population on fluid cells, 0 on solid cells, v0 layout."""
-    u = uniform01(seed, nx * ny * 9)
-    s = (-amp + 2.0 * amp * u).astype(dtype)
+    """f_i - w_i = U(-amp, amp) per population on fluid cells, 0 on solid cells, v0 layout
+    (generated in chunks, so that 8192^2 grids need no multi-GB temporaries)."""
+    n = nx * ny * 9
+    s = np.empty(n, dtype)
+    chunk = 1 << 24
+    for k0 in range(0, n, chunk):
+        k1 = min(n, k0 + chunk)
+        s[k0:k1] = (-amp + 2.0 * amp * uniform01(seed, k1 - k0, offset=k0)).astype(dtype)
     s.reshape(-1, 9)[np.asarray(solid).reshape(-1) != 0] = 0
     return s
 

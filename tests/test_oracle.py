@@ -83,6 +83,21 @@ def test_seeded_generator(orc):
     assert first == -0.5 + (0xE220A8397B1DCDAF >> 11) * 2.0 ** -53
 
 
+def test_package_generator_matches_oracle(pkg, orc):
+    """bench.py draws its synthetic states from the package's generator (chunked, for 8192^2
+    grids); it is the oracle's stream value for value, across chunk boundaries too."""
+    import numpy as np
+    mask = pkg.make_channel(300, 77)
+    for real, dt in (("f32", np.float32), ("f64", np.float64)):
+        assert np.array_equal(pkg.workloads.seeded_state(20240917, 1e-4, 300, 77, mask, dt),
+                              orc.seeded_state(20240917, 1e-4, 300, 77, mask, real))
+    n = (1 << 24) // 9 + 5  # cells whose 9 n values span two generator chunks
+    mask = np.zeros(n, np.uint8)
+    mask[::7] = 1
+    assert np.array_equal(pkg.workloads.seeded_state(3, 0.5, n, 1, mask, np.float32),
+                          orc.seeded_state(3, 0.5, n, 1, mask, "f32"))
+
+
 @pytest.mark.parametrize("name", [n for n in CASES if "seeded" in golden_cases()[n]])
 def test_golden_seeded_state(orc, name):
     case = golden_cases()[name]
