@@ -380,8 +380,10 @@ def run_ours(args):
         pin.numpy()[:] = s_head
         outs = [torch.empty(cells, dtype=tdt).pin_memory() for _ in range(3)]
         with pkg.Solver(n, n, TAU, FX, FY, mask, precision=prec) as s:
+            # One untimed job first: the first large upload and the step graph's capture are
+            # one-time costs of a solver, not of a job.
             s.set_populations(pin.numpy())
-            s.run(10)
+            s.run(E2E_LATTICE_STEPS)
             s.macroscopic([o.numpy() for o in outs])
             barrier(dist)
             torch.cuda.synchronize()
@@ -529,7 +531,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=100)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--nx", type=int, default=4096)
-    ap.add_argument("--e2e-jobs", type=int, default=3)
+    ap.add_argument("--e2e-jobs", type=int, default=5)
     ap.add_argument("--no-forms", dest="forms", action="store_false")
     ap.add_argument("--no-cpu-baseline", dest="cpu_baseline", action="store_false")
     ap.add_argument("--precision", choices=["fp32", "fp64", "fp16", "bf16"], default="fp32",
