@@ -171,8 +171,9 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * 17 = 12 capped for 3 resident blocks; 18 = 17 with 3 stages; 19 = 17 with 1 pass per strip
  * (half-width tiles) and 4 stages. The ring variants are launched with programmatic stream
  * serialisation (the next step's blocks are scheduled while the previous step drains).
- * -1 (the default): 12 (plain FP32 / FP64, 512-cell tiles) or 17 (16-bit storage, 1024-cell
- * tiles) when there are at least two tiles per SM, 0 otherwise.
+ * -1 (the default), by grid size from a sweep on GB300: rows narrower than 256 cells: 0; plain
+ * FP32: 19 below 2^17 cells, 17 below 2^21, 12 above; 16-bit storage: 19 below 2^21 cells, 17
+ * above; FP64: 12 with at least two 512-cell tiles per SM, 0 otherwise.
  * The 16-bit forms round stored populations stochastically (see lbm_create); every variant
  * derives the same random bits, so the variants give the same results. */
 int lbm_set_variant(lbm_solver* s, int variant);

@@ -13,6 +13,8 @@
 //                extracts the G + 2 bits of cells x0 - 1 .. x0 + G with one funnel shift.
 #pragma once
 
+#include <utility>
+
 #include <cuda_bf16.h>
 #include <cuda_fp16.h>
 #include <cuda_runtime.h>
@@ -530,5 +532,33 @@ template <class T>
 struct Eq9 {
   T v[kQ];
 };
+
+// ---------------------------------------------------------------------------------------------
+// Programmatic dependent launch, device side: wait until the previous kernel on the stream has
+// completed and its writes are visible (a no-op for a kernel launched without the attribute),
+// then let the next kernel's blocks be scheduled as this one's exit.
+__device__ __forceinline__ void grid_dependency_wait() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
+// Host side: a launch with programmatic stream serialisation, so that its blocks may be
+// scheduled while the previous kernel on the stream drains (they start with
+// grid_dependency_wait before touching memory).
+template <class... Params, class... Args>
+cudaError_t launch_dependent(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
+                             Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = stream;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
 
 }  // namespace lbm_b200

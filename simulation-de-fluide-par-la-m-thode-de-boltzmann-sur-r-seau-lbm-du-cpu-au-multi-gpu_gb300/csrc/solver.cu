@@ -99,7 +99,7 @@ int launch_steps_t(lbm_solver* s, int steps) {
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
     a.step_ctr = s->step_ctr;
     a.step_off = static_cast<uint32_t>(k);
-    kernel<<<grid, s->block, 0, s->stream>>>(a);
+    LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(s->block), 0, s->stream, a));
     s->cur ^= 1;
   }
   LBM_CUDA(s, cudaGetLastError());
@@ -139,7 +139,8 @@ int launch_tma_t(lbm_solver* s, int steps) {
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
     a.step_ctr = s->step_ctr;
     a.step_off = static_cast<uint32_t>(k);
-    kernel<<<grid, kTmaThreads, smem, s->stream>>>(a, tpr, tiles, s->err_flag);
+    LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(kTmaThreads), smem, s->stream, a, tpr, tiles,
+                                 s->err_flag));
     s->cur ^= 1;
   }
   LBM_CUDA(s, cudaGetLastError());
@@ -179,7 +180,7 @@ int launch_async_t(lbm_solver* s, int steps) {
     a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
     a.step_ctr = s->step_ctr;
     a.step_off = static_cast<uint32_t>(k);
-    kernel<<<grid, kBlock, smem, s->stream>>>(a);
+    LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(kBlock), smem, s->stream, a));
     s->cur ^= 1;
   }
   LBM_CUDA(s, cudaGetLastError());
@@ -228,16 +229,25 @@ int launch_ring_t(lbm_solver* s, int steps) {
   }
 }
 
-// Automatic kernel choice (variant < 0): the ring kernel when there are at least two of its
-// tiles per SM (plain FP32 / FP64: 12, 63 registers, 3 resident blocks; 16-bit storage: 17, the
-// same shape capped at 72 registers for 3 resident blocks), the direct kernel (0) otherwise
-// (small grids, where most consumer warps would idle).
+// Automatic kernel choice (variant < 0), from a sweep of every variant on one GB300 (channel,
+// best of 3 runs, MLUPS): plain FP32: 256^2 v19 20.8k (v0 19.8k), 512^2 / 1024x256 v17 51.9k /
+// 51.7k (v12 47.4k / 46.2k), 1024^2 v17 83.9k (v12 81.7k), 2048^2 v12 86.2k, 4096^2 v12 90.6k;
+// 16-bit storage: 256^2 v19 20.2k (v0 13.5k), 512^2 v19 61.2k, 1024^2 v19 114.4k (v17 109.6k),
+// 2048^2 v17 138.3k (v14 142.7k), 4096^2 v17 158.2k. Rows narrower than 256 cells take the
+// direct kernel (0), whose 128-cell chunks leave fewer lanes idle than the rings' wide tiles
+// (FP64 on 100 x 2000: the ring 12 reached 1.0k MLUPS with a fifth of its lanes busy); otherwise
+// FP64 (FP64-ALU-bound) takes the ring 12 with at least two of its tiles per SM, else 0.
 template <class ST>
 int auto_variant(const lbm_solver* s) {
   using S = RingShape<ST, 8, 2>;
-  const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
-  if (tiles < 2LL * s->sm_count) return 0;
-  return sizeof(ST) == 2 ? 17 : 12;
+  const long long cells = static_cast<long long>(s->nx) * s->ny;
+  if (s->nx < 256) return 0;
+  if (sizeof(ST) == 8) {
+    const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
+    return tiles < 2LL * s->sm_count ? 0 : 12;
+  }
+  if (sizeof(ST) == 2) return cells < (2LL << 20) ? 19 : 17;
+  return cells < (1LL << 17) ? 19 : (cells < (2LL << 20) ? 17 : 12);
 }
 
 template <class ST, bool kOpen>

@@ -96,6 +96,7 @@ template <class ST, class Phys, bool kOpen, int kDepth>
 __global__ void __launch_bounds__(128) async_step_kernel(const StepArgs<ST, Phys> p) {
   using S = AsyncShape<ST>;
   extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int wpb = blockDim.x >> 5;
   unsigned char* ring = smem + static_cast<size_t>(warp) * kDepth * S::kStageBytes;

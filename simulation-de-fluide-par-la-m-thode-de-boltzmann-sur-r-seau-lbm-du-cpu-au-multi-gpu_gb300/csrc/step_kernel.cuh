@@ -302,6 +302,7 @@ __global__ void __launch_bounds__(kStepThreads, VariantTraits<kVariant>::min_blo
     pull_step_kernel(const StepArgs<ST, Phys> p) {
   using T = typename StoreTraits<ST>::T;
   constexpr int G = StoreTraits<ST>::kVec;
+  grid_dependency_wait();
   const int lane = threadIdx.x & 31;
   const int nwarps = (gridDim.x * blockDim.x) >> 5;
   int item = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;

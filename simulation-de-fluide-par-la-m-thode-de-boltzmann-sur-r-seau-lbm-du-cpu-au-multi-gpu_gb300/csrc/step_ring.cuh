@@ -460,33 +460,6 @@ struct GridTiles {
   }
 };
 
-// Programmatic dependent launch, device side: wait until the previous kernel on the stream has
-// completed and its writes are visible (a no-op for a kernel launched without the attribute),
-// then let the next kernel's blocks be scheduled as this one's exit.
-__device__ __forceinline__ void grid_dependency_wait() {
-  asm volatile("griddepcontrol.wait;" ::: "memory");
-  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
-}
-
-// Host side: a launch with programmatic stream serialisation, so that its blocks may be
-// scheduled while the previous kernel on the stream drains (they start with
-// grid_dependency_wait before touching memory).
-template <class... Params, class... Args>
-cudaError_t launch_dependent(void (*kernel)(Params...), dim3 grid, dim3 block, size_t smem, cudaStream_t stream,
-                             Args&&... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = block;
-  cfg.dynamicSmemBytes = smem;
-  cfg.stream = stream;
-  cudaLaunchAttribute attr[1];
-  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  attr[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = attr;
-  cfg.numAttrs = 1;
-  return cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
-}
-
 template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
     ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int row0, int* err) {

@@ -276,6 +276,7 @@ __global__ void __launch_bounds__(kTmaThreads, kStages <= 3 ? 2 : 1)
     tma_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int* err) {
   using S = TmaShape<ST>;
   extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
   // Stage s: 9 plane rows (kPlaneBytes) then 3 mask rows (3 * MW words).
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * S::kStageBytes);
   uint64_t* empty = full + kStages;
