@@ -421,8 +421,9 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
 }
 
 // The step pipeline of one tile visitor (`tiles_of.visit(tile, f)` calls f(p, y, tx0) with the
-// grid, row and first cell of a tile: one grid for the solver, the tile's instance for the
-// batched ensemble).
+// grid, row and first cell of a tile; GridTiles below for the solver and the strip engine).
+// The batched ensemble and the adjoint use tile_pipeline with their own stage policies
+// (batch.cu, adjoint.cu).
 template <class ST, class Phys, bool kOpen, int kW, int kC, class Tiles>
 struct StepPolicy {
   using S = RingShape<ST, kW, kC>;
