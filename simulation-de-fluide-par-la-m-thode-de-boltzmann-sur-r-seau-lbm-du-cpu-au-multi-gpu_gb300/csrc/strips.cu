@@ -7,8 +7,9 @@
 //   * decomposition as the reference's make_strip: strip k owns ny / S rows, the first ny % S
 //     strips one more (at least 2 rows each); its buffers hold local rows 0 .. n_k + 1, row 0 and
 //     row n_k + 1 being the ghost copies of global rows y0 - 1 and y0 + n_k (periodic ring);
-//   * one step = the ring step kernel on the owned rows of every strip (rows 1 .. n_k, whose
-//     y-neighbours are all local), then one halo launch for all strips: the ghost row below
+//   * one step = one launch of the ring step kernel over the owned rows of every strip (rows
+//     1 .. n_k, whose y-neighbours are all local; a tile finds its strip by binary search over
+//     the strips' first tiles), then one halo launch for all strips: the ghost row below
 //     strip k receives the populations moving up (c_y = +1: 2, 5, 6) of the top owned row of the
 //     strip below, the ghost row above receives those moving down (c_y = -1: 4, 7, 8) of the
 //     bottom owned row of the strip above: 3 * nx values per message, the reference's halo
@@ -50,11 +51,71 @@ struct StripView {
   int n;            // owned rows
 };
 
+// A strip as the step kernel sees it: offsets of its planes and mask rows, its rounding-key
+// base (cell offset of global row y0 - 1), owned rows and first tile of the step's tile index.
+struct StripTile {
+  long long off, plane, key_base, moff;
+  int n, tile0;
+};
+constexpr int kStripTableSmem = 256;  // strip tables up to this size are staged in shared memory
+
+// Tiles of all strips for the ring pipeline: tpr tiles per row, the owned rows of strip 0, then
+// of strip 1, ...; the grid of a tile is the strip's (base arguments with the strip's offsets).
+template <class ST, class Phys, int kTW>
+struct StripTiles {
+  const StepArgs<ST, Phys>& base;  // src / dst / mask: buffer bases; g: nx, pitch, mask words
+  const StripTile* tab;
+  int strips, tpr;
+  template <class F>
+  __device__ __forceinline__ void visit(int tile, F&& f) const {
+    int lo = 0, hi = strips - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (tab[mid].tile0 <= tile)
+        lo = mid;
+      else
+        hi = mid - 1;
+    }
+    const StripTile& t = tab[lo];
+    StepArgs<ST, Phys> p = base;
+    p.src = base.src + t.off;
+    p.dst = base.dst + t.off;
+    p.mask = base.mask + t.moff;
+    p.g.ny = t.n + 2;
+    p.g.plane = t.plane;
+    p.key_base = t.key_base;
+    const int local = tile - t.tile0;
+    const int r = local / tpr;
+    f(p, r + 1, (local - r * tpr) * kTW);
+  }
+};
+
+// One step of every strip: the solver's ring kernel (8 consumer warps x 2 passes, 2 stages)
+// over the strips' tiles.
+template <class ST, class Phys, bool kOpen, int kMinBlocks>
+__global__ void __launch_bounds__(32 * 9, kMinBlocks)
+    strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips, int tpr,
+                      int tiles, int* err) {
+  using S = RingShape<ST, 8, 2>;
+  extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
+  const StripTile* t = tab;
+  if (strips <= kStripTableSmem) {
+    StripTile* s_tab = reinterpret_cast<StripTile*>(smem + ring_smem_bytes<S>(2));
+    for (int k = threadIdx.x; k < strips; k += blockDim.x) s_tab[k] = tab[k];
+    __syncthreads();
+    t = s_tab;
+  }
+  const StripTiles<ST, Phys, S::TW> tiles_of{base, t, strips, tpr};
+  ring_pipeline<ST, Phys, kOpen, 8, 2, 2>(smem, tiles_of, tiles, err);
+}
+
 // Device halo exchange of all strips (raw elements E, the storage bits): thread per
 // (strip, one of 6 (direction, plane) pairs, column).
 template <class E>
 __global__ void strip_halo_kernel(E* __restrict__ buf, const StripView* __restrict__ v, int strips,
                                   int nx, int pitch) {
+  grid_dependency_wait();
   const long long total = static_cast<long long>(strips) * 6 * nx;
   for (long long t = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; t < total;
        t += static_cast<long long>(gridDim.x) * blockDim.x) {
@@ -91,6 +152,7 @@ struct lbm_strips {
   int cur = 0;
   uint32_t* mask_d = nullptr;
   StripView* views_d = nullptr;
+  StripTile* tiles_d = nullptr;  // the step kernel's strip table
   uint32_t* ctr = nullptr;  // [0]: step counter, [1]: error flag of the bounded waits
   void* stage = nullptr;
   size_t stage_bytes = 0;
@@ -154,51 +216,44 @@ template <class ST>
 int halo_t(lbm_strips* h, int b) {
   using E = std::conditional_t<sizeof(ST) == 2, uint16_t, std::conditional_t<sizeof(ST) == 4, uint32_t, uint64_t>>;
   const long long total = static_cast<long long>(h->strips) * 6 * h->nx;
-  strip_halo_kernel<E><<<grid_cells(h, total), 256, 0, h->stream>>>(static_cast<E*>(h->buf[b]), h->views_d,
-                                                                     h->strips, h->nx, h->pitch);
-  S_CUDA(h, cudaGetLastError());
+  S_CUDA(h, launch_dependent(strip_halo_kernel<E>, dim3(grid_cells(h, total)), dim3(256), 0, h->stream,
+                             static_cast<E*>(h->buf[b]), static_cast<const StripView*>(h->views_d), h->strips,
+                             h->nx, h->pitch));
   return LBM_OK;
 }
 
-// `steps` steps: per step, the ring kernel on every strip's owned rows, then the halo exchange
-// into the state just written; then the step counter advances.
+// `steps` steps: per step, one ring launch over every strip's owned rows, then the halo
+// exchange into the state just written; then the step counter advances.
 template <class ST, bool kOpen>
 int steps_t(lbm_strips* h, int steps) {
   using Phys = typename Form<ST>::Phys;
   using T = typename StoreTraits<ST>::T;
   constexpr int kMin = sizeof(ST) == 2 ? 3 : 1;  // as the solver's variants 17 / 12
   using S = RingShape<ST, 8, 2>;
-  const auto kernel = ring_step_kernel<ST, Phys, kOpen, 8, 2, 2, kMin>;
-  const size_t smem = ring_smem_bytes<S>(2);
+  const auto kernel = strip_ring_kernel<ST, Phys, kOpen, kMin>;
+  const size_t smem = ring_smem_bytes<S>(2) +
+                      (h->strips <= kStripTableSmem ? h->strips * sizeof(StripTile) : 0);
   S_CUDA(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
   S_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, S::kThreads, smem));
   const int tpr = (h->nx + S::TW - 1) / S::TW;
+  const int tiles = tpr * h->ny;  // the strips' owned rows cover the lattice once
+  const int grid = std::max(1, std::min(tiles, std::max(1, per_sm) * h->sm_count));
   const Eq9<T> e = strip_inlet<ST>(h, true);
-  std::vector<StepArgs<ST, Phys>> args(h->strips);
-  std::vector<int> grids(h->strips);
-  for (int k = 0; k < h->strips; ++k) {
-    StepArgs<ST, Phys>& a = args[k];
-    a = StepArgs<ST, Phys>{};
-    a.mask = h->mask_d + h->moff[k];
-    a.g = strip_grid(h, k);
-    a.k = Form<ST>::consts(h->tau, h->fx, h->fy);
-    for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
-    a.sc = h->sc;
-    a.step_ctr = h->ctr;
-    a.key_base = static_cast<long long>(h->y0[k] - 1) * h->pitch;  // local row 1 = global row y0
-    grids[k] = std::max(1, std::min(tpr * h->n[k], std::max(1, per_sm) * h->sm_count));
-  }
+  StepArgs<ST, Phys> a{};
+  a.mask = h->mask_d;
+  a.g = strip_grid(h, 0);
+  a.k = Form<ST>::consts(h->tau, h->fx, h->fy);
+  for (int i = 0; i < kQ; ++i) a.eq_in[i] = e.v[i];
+  a.sc = h->sc;
+  a.step_ctr = h->ctr;
   int* err = reinterpret_cast<int*>(h->ctr + 1);
   for (int s = 0; s < steps; ++s) {
-    const ST* src = static_cast<const ST*>(h->buf[h->cur]);
-    ST* dst = static_cast<ST*>(h->buf[h->cur ^ 1]);
-    for (int k = 0; k < h->strips; ++k) {
-      args[k].src = src + h->off[k];
-      args[k].dst = dst + h->off[k];
-      args[k].step_off = static_cast<uint32_t>(s);
-      kernel<<<grids[k], S::kThreads, smem, h->stream>>>(args[k], tpr, tpr * h->n[k], 1, err);
-    }
+    a.src = static_cast<const ST*>(h->buf[h->cur]);
+    a.dst = static_cast<ST*>(h->buf[h->cur ^ 1]);
+    a.step_off = static_cast<uint32_t>(s);
+    S_CUDA(h, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, h->stream, a,
+                               static_cast<const StripTile*>(h->tiles_d), h->strips, tpr, tiles, err));
     if (int rc = halo_t<ST>(h, h->cur ^ 1)) return rc;
     h->cur ^= 1;
   }
@@ -456,6 +511,21 @@ int lbm_strips_create(int nx, int ny, const uint8_t* solid, double tau, double f
     e = cudaMemcpy(h->mask_d, all_words.data(), all_words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&h->views_d, strips * sizeof(StripView));
   if (e == cudaSuccess) e = cudaMemcpy(h->views_d, views.data(), strips * sizeof(StripView), cudaMemcpyHostToDevice);
+  // The step kernel's strip table: tiles of the ring shape (8 consumer warps x 2 passes: 512
+  // cells per tile, 1024 with 16-bit storage) over the owned rows, strip after strip.
+  {
+    const int tw = 32 * 8 * 2 * (elem == 2 ? 2 : 1);
+    const int tpr = (nx + tw - 1) / tw;
+    std::vector<StripTile> tt(strips);
+    int tile0 = 0;
+    for (int k = 0; k < strips; ++k) {
+      tt[k] = StripTile{h->off[k], views[k].plane, static_cast<long long>(h->y0[k] - 1) * h->pitch, h->moff[k],
+                        h->n[k], tile0};
+      tile0 += tpr * h->n[k];
+    }
+    if (e == cudaSuccess) e = cudaMalloc(&h->tiles_d, strips * sizeof(StripTile));
+    if (e == cudaSuccess) e = cudaMemcpy(h->tiles_d, tt.data(), strips * sizeof(StripTile), cudaMemcpyHostToDevice);
+  }
   if (e == cudaSuccess) e = cudaMalloc(&h->ctr, 4 * sizeof(uint32_t));
   if (e == cudaSuccess) e = cudaMemset(h->ctr, 0, 4 * sizeof(uint32_t));
   if (e != cudaSuccess) return fail(e == cudaErrorMemoryAllocation ? LBM_ERR_OUT_OF_MEMORY : LBM_ERR_CUDA);
@@ -468,7 +538,7 @@ int lbm_strips_destroy(lbm_strips* h) {
   if (h->stream) cudaStreamSynchronize(h->stream);
   drop_graph(h);
   for (void* p : {h->buf[0], h->buf[1], static_cast<void*>(h->mask_d), static_cast<void*>(h->views_d),
-                  static_cast<void*>(h->ctr), h->stage})
+                  static_cast<void*>(h->tiles_d), static_cast<void*>(h->ctr), h->stage})
     cudaFree(p);
   for (cudaEvent_t ev : h->ev)
     if (ev) cudaEventDestroy(ev);
