@@ -354,8 +354,10 @@ def run_ours(args):
     barrier(dist)
     torch.cuda.synchronize()
     solver.synchronize()
+    k_before = solver.kernel_launches()
     t_start = time.time()
     secs = solver.timed_run(args.steps)
+    launches = solver.kernel_launches() - k_before
     torch.cuda.synchronize()
     barrier(dist)
     sampler.window = (t_start, time.time())
@@ -387,11 +389,19 @@ def run_ours(args):
             s.macroscopic([o.numpy() for o in outs])
             barrier(dist)
             torch.cuda.synchronize()
+            phase = [0.0, 0.0, 0.0]  # upload, lattice steps, moments + download (each call synchronises)
             t0 = time.perf_counter()
             for _ in range(args.e2e_jobs):
+                ta = time.perf_counter()
                 s.set_populations(pin.numpy())
+                tb = time.perf_counter()
                 s.run(E2E_LATTICE_STEPS)
+                tc = time.perf_counter()
                 s.macroscopic([o.numpy() for o in outs])
+                td = time.perf_counter()
+                phase[0] += tb - ta
+                phase[1] += tc - tb
+                phase[2] += td - tc
             torch.cuda.synchronize()
             barrier(dist)
             dt = max_over_ranks(time.perf_counter() - t0, dist)
@@ -399,7 +409,10 @@ def run_ours(args):
                "unit": "MLUPS", "h2d_bytes_per_step": int(s_head.nbytes),
                "d2h_bytes_per_step": int(3 * cells * s_head.itemsize),
                "lattice_steps_per_e2e_step": E2E_LATTICE_STEPS, "e2e_steps": args.e2e_jobs,
-               "api": "lbm_set_populations + lbm_run(1000) + lbm_macroscopic (C ABI)"}
+               "api": "lbm_set_populations + lbm_run(1000) + lbm_macroscopic (C ABI)",
+               "phase_ms_per_step": {"upload": round(1e3 * phase[0] / args.e2e_jobs, 2),
+                                     "lattice_steps": round(1e3 * phase[1] / args.e2e_jobs, 2),
+                                     "download": round(1e3 * phase[2] / args.e2e_jobs, 2)}}
 
     forms = {}
     if args.forms and rank == 0:
@@ -458,7 +471,7 @@ def run_ours(args):
                      "traffic": traffic, "peak_kind": peak_kind,
                      "algorithmic_bytes_per_launch": BYTES_PER_CELL[prec] * cells},
         "clocks": sampler.summary(),
-        "gpu_launches": args.steps,
+        "gpu_launches": launches,
         "e2e": e2e,
         "cpu_baseline": cpu,
         "forms": forms or None,

@@ -110,6 +110,11 @@ int lbm_timed_run(lbm_solver* s, int steps, double* seconds);
 /* Waits for all work of s. */
 int lbm_synchronize(lbm_solver* s);
 
+/* Number of kernels s has enqueued for time steps so far: one per step plus one step-counter
+ * update per launch sequence (a replayed step graph counts the kernels it holds). For
+ * benchmarks that report how many of the library's kernels ran in a timed region. */
+int lbm_kernel_launches(const lbm_solver* s, long long* count);
+
 /* Replaces SolverV3::populations() (solver_v3.cu:300-320): post-streaming populations in v0
  * layout into s_host (nx*ny*9 values of the host type), solid cells 0. The gather runs on the
  * device. */

@@ -92,6 +92,7 @@ def lib() -> C.CDLL:
             "lbm_adj_backward": ([vp, vp, vp, vp, vp], i),
             "lbm_adj_get_populations": ([vp, i, vp], i),
             "lbm_adj_step_times": ([vp, C.POINTER(d), C.POINTER(d)], i),
+            "lbm_kernel_launches": ([vp, C.POINTER(C.c_longlong)], i),
             "lbm_adj_set_tiles": ([vp, i, i], i),
             "lbm_adj_get_tiles": ([vp, C.POINTER(i), C.POINTER(i)], i),
             "lbm_batch_create": ([i, vp, vp, vp, vp, vp, vp, i, C.POINTER(vp)], i),
@@ -238,6 +239,12 @@ class Solver:
 
     def threads(self) -> int:
         return 0
+
+    def kernel_launches(self) -> int:
+        """Kernels enqueued for time steps so far (step launches and step-counter updates)."""
+        n = C.c_longlong(0)
+        self._check(lib().lbm_kernel_launches(self._h, C.byref(n)))
+        return n.value
 
     def bench_info(self) -> str:
         buf = C.create_string_buffer(1024)

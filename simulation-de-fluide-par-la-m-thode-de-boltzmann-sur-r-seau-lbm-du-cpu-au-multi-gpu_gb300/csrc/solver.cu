@@ -465,10 +465,14 @@ int solver_step_raw(lbm_solver* s, int steps) {
     if (int rc = ensure_step_graph(s)) return rc;
     while (s->graph && steps >= kGraphSteps) {
       LBM_CUDA(s, cudaGraphLaunch(s->graph, s->stream));
+      s->kernels += kGraphSteps + 1;  // the graph's step launches and its step-counter update
       steps -= kGraphSteps;
     }
   }
-  return steps > 0 ? solver_launch(s, steps) : LBM_OK;
+  if (steps <= 0) return LBM_OK;
+  const int rc = solver_launch(s, steps);
+  if (!rc) s->kernels += steps + 1;
+  return rc;
 }
 
 int solver_mass_into(lbm_solver* s, const void* state, double* partials, int blocks,
@@ -680,6 +684,12 @@ int lbm_synchronize(lbm_solver* s) {
 int lbm_run(lbm_solver* s, int steps) {
   if (int rc = lbm_step(s, steps)) return rc;
   return lbm_synchronize(s);
+}
+
+int lbm_kernel_launches(const lbm_solver* s, long long* count) {
+  if (!s || !count) return LBM_ERR_INVALID_ARG;
+  *count = s->kernels;
+  return LBM_OK;
 }
 
 int lbm_timed_run(lbm_solver* s, int steps, double* seconds) {

@@ -21,6 +21,7 @@ struct lbm_solver {
   cudaGraphExec_t graph = nullptr;  // kGraphSteps step launches (see solver_step_raw)
   int graph_cur = -1;               // buffer parity the graph was captured from
   bool graphs = true;               // false after a failed capture
+  long long kernels = 0;            // kernels enqueued by steps (step launches and counter updates)
   size_t state_bytes = 0;
   uint32_t* mask_d = nullptr;  // bit-packed mask with periodic ghost bits
   uint32_t* body_d = nullptr;  // bit-packed body of lbm_body_force (null: every solid cell)

@@ -102,3 +102,19 @@ def test_graph_replay_equals_single_launches(gpu_lib, form):
         for _ in range(203):
             b.step(1)
         assert np.array_equal(a.populations(), b.populations())
+
+
+def test_kernel_launch_count(gpu_lib):
+    """lbm_kernel_launches counts what a run enqueues: one kernel per step and one step-counter
+    update per launch sequence (a replayed 32-step graph holds 33 kernels). bench.py reports
+    its timed region's gpu_launches from it."""
+    nx, ny = 300, 70
+    mask = gpu_lib.make_channel(nx, ny)
+    with gpu_lib.Solver(nx, ny, 0.6, 1e-6, 0.0, mask) as s:
+        s.init_equilibrium(1.0, 0.0, 0.0)
+        k0 = s.kernel_launches()
+        s.run(5)
+        assert s.kernel_launches() - k0 == 6
+        k1 = s.kernel_launches()
+        s.run(200)  # 6 graphs of 32 steps + 8 direct steps
+        assert s.kernel_launches() - k1 in (6 * 33 + 9, 200 + 1)
