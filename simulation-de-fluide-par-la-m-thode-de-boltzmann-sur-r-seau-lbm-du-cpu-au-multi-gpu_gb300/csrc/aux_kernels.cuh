@@ -200,6 +200,15 @@ __global__ void finite_kernel(const ST* __restrict__ R, const uint32_t* __restri
 // sequence, inside a captured graph as well.
 static __global__ void counter_add_kernel(uint32_t* c, uint32_t n) { *c += n; }
 
+// Copy of n16 16-byte words with coalesced vector loads and stores (a host buffer that kernels
+// can address, e.g. pinned memory over NVLink-C2C, into device memory: the SMs' loads keep more
+// bytes in flight than a copy engine on some hosts).
+static __global__ void copy16_kernel(const uint4* __restrict__ src, uint4* __restrict__ dst, long long n16) {
+  for (long long k = blockIdx.x * static_cast<long long>(blockDim.x) + threadIdx.x; k < n16;
+       k += static_cast<long long>(gridDim.x) * blockDim.x)
+    dst[k] = src[k];
+}
+
 // Momentum-exchange force on a body (halfway bounce-back, stationary walls): every link from a
 // fluid cell x to a body cell x + c_i carries 2 c_i f*_i(x), with f*_i(x) = R_i(x) + w_i the
 // post-collision population of x leaving along c_i (the pull state holds post-collision

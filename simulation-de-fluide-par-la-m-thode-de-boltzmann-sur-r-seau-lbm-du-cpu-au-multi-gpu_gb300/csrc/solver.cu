@@ -637,17 +637,40 @@ int lbm_init_equilibrium(lbm_solver* s, double rho0, double ux0, double uy0) {
   LBM_DISPATCH(s, init_eq_t, s, rho0, ux0, uy0);
 }
 
+// Device address of a host buffer that kernels may access directly (pinned or registered host
+// memory, e.g. over NVLink-C2C), or null: pageable memory is staged through device memory.
+static const void* mapped_view(const void* p) {
+  cudaPointerAttributes a{};
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? a.devicePointer : nullptr;
+}
+
 int lbm_set_populations(lbm_solver* s, const void* s_host) {
   if (check(s) || !s_host) return set_error(s, LBM_ERR_INVALID_ARG, "null state");
   const size_t bytes = static_cast<size_t>(s->nx) * s->ny * kQ * s->host_elem;
+  // One copy into device memory, then the conversion kernel (whose neighbour gathers would be
+  // slow over the host link): from pinned host memory with coalesced 16-byte kernel loads
+  // (size and address permitting), else with a copy engine.
   if (int rc = ensure_stage(s, bytes)) return rc;
-  LBM_CUDA(s, cudaMemcpyAsync(s->stage, s_host, bytes, cudaMemcpyHostToDevice, s->stream));
+  const void* mapped = mapped_view(s_host);
+  if (mapped && bytes % 16 == 0 && reinterpret_cast<uintptr_t>(mapped) % 16 == 0) {
+    const long long n16 = static_cast<long long>(bytes / 16);
+    copy16_kernel<<<grid_for_cells(s, n16, 256), 256, 0, s->stream>>>(static_cast<const uint4*>(mapped),
+                                                                      static_cast<uint4*>(s->stage), n16);
+    LBM_CUDA(s, cudaGetLastError());
+  } else {
+    LBM_CUDA(s, cudaMemcpyAsync(s->stage, s_host, bytes, cudaMemcpyHostToDevice, s->stream));
+  }
+  const void* src = s->stage;
   int rc;
   switch (s->precision) {
-    case LBM_FP32: rc = set_state_t<float>(s, s->stage, Eq9<float>{}); break;
-    case LBM_FP64: rc = set_state_t<double>(s, s->stage, Eq9<double>{}); break;
-    case LBM_FP16_STORE: rc = set_state_t<__half>(s, s->stage, Eq9<float>{}); break;
-    case LBM_BF16_STORE: rc = set_state_t<__nv_bfloat16>(s, s->stage, Eq9<float>{}); break;
+    case LBM_FP32: rc = set_state_t<float>(s, src, Eq9<float>{}); break;
+    case LBM_FP64: rc = set_state_t<double>(s, src, Eq9<double>{}); break;
+    case LBM_FP16_STORE: rc = set_state_t<__half>(s, src, Eq9<float>{}); break;
+    case LBM_BF16_STORE: rc = set_state_t<__nv_bfloat16>(s, src, Eq9<float>{}); break;
     default: rc = LBM_ERR_INVALID_ARG;
   }
   if (rc) return rc;
@@ -663,7 +686,7 @@ int lbm_step(lbm_solver* s, int steps) {
 }
 
 // Reads and clears the device error flag of the step kernels (a bounded wait that ran out).
-int check_step_flag(lbm_solver* s) {
+static int check_step_flag(lbm_solver* s) {
   int flag = 0;
   LBM_CUDA(s, cudaMemcpyAsync(&flag, s->err_flag, sizeof(int), cudaMemcpyDeviceToHost, s->stream));
   LBM_CUDA(s, cudaStreamSynchronize(s->stream));
@@ -707,17 +730,23 @@ int lbm_timed_run(lbm_solver* s, int steps, double* seconds) {
 int lbm_get_populations(lbm_solver* s, void* s_host) {
   if (check(s) || !s_host) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
   const size_t bytes = static_cast<size_t>(s->nx) * s->ny * kQ * s->host_elem;
-  if (int rc = ensure_stage(s, bytes)) return rc;
+  // Pinned host output: the gather kernel writes it in place; else through device memory.
+  void* dst = const_cast<void*>(mapped_view(s_host));
+  if (!dst) {
+    if (int rc = ensure_stage(s, bytes)) return rc;
+    dst = s->stage;
+  }
   int rc;
   switch (s->precision) {
-    case LBM_FP32: rc = get_state_t<float>(s, s->stage); break;
-    case LBM_FP64: rc = get_state_t<double>(s, s->stage); break;
-    case LBM_FP16_STORE: rc = get_state_t<__half>(s, s->stage); break;
-    case LBM_BF16_STORE: rc = get_state_t<__nv_bfloat16>(s, s->stage); break;
+    case LBM_FP32: rc = get_state_t<float>(s, dst); break;
+    case LBM_FP64: rc = get_state_t<double>(s, dst); break;
+    case LBM_FP16_STORE: rc = get_state_t<__half>(s, dst); break;
+    case LBM_BF16_STORE: rc = get_state_t<__nv_bfloat16>(s, dst); break;
     default: rc = LBM_ERR_INVALID_ARG;
   }
   if (rc) return rc;
-  LBM_CUDA(s, cudaMemcpyAsync(s_host, s->stage, bytes, cudaMemcpyDeviceToHost, s->stream));
+  if (dst == s->stage)
+    LBM_CUDA(s, cudaMemcpyAsync(s_host, s->stage, bytes, cudaMemcpyDeviceToHost, s->stream));
   LBM_CUDA(s, cudaStreamSynchronize(s->stream));
   return LBM_OK;
 }
@@ -726,20 +755,34 @@ int lbm_macroscopic(lbm_solver* s, void* rho, void* ux, void* uy) {
   if (check(s) || !rho || !ux || !uy) return set_error(s, LBM_ERR_INVALID_ARG, "null output");
   const size_t n = static_cast<size_t>(s->nx) * s->ny;
   const size_t plane = n * s->host_elem;
-  if (int rc = ensure_stage(s, std::max(3 * plane, n * kQ * s->host_elem))) return rc;
-  char* d = static_cast<char*>(s->stage);
+  // Pinned host outputs (all three): the moment kernel writes them in place; else through
+  // device memory.
+  void* mr = const_cast<void*>(mapped_view(rho));
+  void* mu = const_cast<void*>(mapped_view(ux));
+  void* mv = const_cast<void*>(mapped_view(uy));
+  const bool direct = mr && mu && mv;
+  char* d = nullptr;
+  if (!direct) {
+    if (int rc = ensure_stage(s, std::max(3 * plane, n * kQ * s->host_elem))) return rc;
+    d = static_cast<char*>(s->stage);
+    mr = d;
+    mu = d + plane;
+    mv = d + 2 * plane;
+  }
   int rc;
   switch (s->precision) {
-    case LBM_FP32: rc = moments_t<float>(s, d, d + plane, d + 2 * plane); break;
-    case LBM_FP64: rc = moments_t<double>(s, d, d + plane, d + 2 * plane); break;
-    case LBM_FP16_STORE: rc = moments_t<__half>(s, d, d + plane, d + 2 * plane); break;
-    case LBM_BF16_STORE: rc = moments_t<__nv_bfloat16>(s, d, d + plane, d + 2 * plane); break;
+    case LBM_FP32: rc = moments_t<float>(s, mr, mu, mv); break;
+    case LBM_FP64: rc = moments_t<double>(s, mr, mu, mv); break;
+    case LBM_FP16_STORE: rc = moments_t<__half>(s, mr, mu, mv); break;
+    case LBM_BF16_STORE: rc = moments_t<__nv_bfloat16>(s, mr, mu, mv); break;
     default: rc = LBM_ERR_INVALID_ARG;
   }
   if (rc) return rc;
-  LBM_CUDA(s, cudaMemcpyAsync(rho, d, plane, cudaMemcpyDeviceToHost, s->stream));
-  LBM_CUDA(s, cudaMemcpyAsync(ux, d + plane, plane, cudaMemcpyDeviceToHost, s->stream));
-  LBM_CUDA(s, cudaMemcpyAsync(uy, d + 2 * plane, plane, cudaMemcpyDeviceToHost, s->stream));
+  if (!direct) {
+    LBM_CUDA(s, cudaMemcpyAsync(rho, d, plane, cudaMemcpyDeviceToHost, s->stream));
+    LBM_CUDA(s, cudaMemcpyAsync(ux, d + plane, plane, cudaMemcpyDeviceToHost, s->stream));
+    LBM_CUDA(s, cudaMemcpyAsync(uy, d + 2 * plane, plane, cudaMemcpyDeviceToHost, s->stream));
+  }
   LBM_CUDA(s, cudaStreamSynchronize(s->stream));
   return LBM_OK;
 }

@@ -118,3 +118,29 @@ def test_kernel_launch_count(gpu_lib):
         k1 = s.kernel_launches()
         s.run(200)  # 6 graphs of 32 steps + 8 direct steps
         assert s.kernel_launches() - k1 in (6 * 33 + 9, 200 + 1)
+
+
+@pytest.mark.parametrize("form", ["fp32", "fp64", "fp16"])
+def test_pinned_host_buffers_equal_pageable(gpu_lib, orc, form):
+    """Pinned host buffers are read / written in place by the conversion, gather and moment
+    kernels; pageable ones go through device memory. Both give the same values."""
+    torch = pytest.importorskip("torch")
+    nx, ny = 300, 70
+    mask = gpu_lib.workloads.cylinder_wake(nx, ny, d=12.0, xc=60.0, yc=36.0)
+    real, tdt = ("f64", torch.float64) if form == "fp64" else ("f32", torch.float32)
+    s0 = orc.seeded_state(11, 1e-3, nx, ny, mask, real)
+    pin = torch.from_numpy(s0.copy()).pin_memory()
+    outs = [torch.empty(nx * ny, dtype=tdt).pin_memory() for _ in range(3)]
+    pops = torch.empty(nx * ny * 9, dtype=tdt).pin_memory()
+    with gpu_lib.Solver(nx, ny, 0.56, 2e-6, 0.0, mask, precision=form) as a, \
+            gpu_lib.Solver(nx, ny, 0.56, 2e-6, 0.0, mask, precision=form) as b:
+        a.set_populations(pin.numpy())
+        b.set_populations(s0)
+        a.run(40)
+        b.run(40)
+        a.macroscopic([o.numpy() for o in outs])
+        want = b.macroscopic()
+        for got, w in zip(outs, want):
+            assert np.array_equal(got.numpy(), w)
+        a.populations(pops.numpy())
+        assert np.array_equal(pops.numpy(), b.populations())
