@@ -22,6 +22,9 @@
  *     8: (+,-) (src/common/d2q9.hpp:14-25).
  *   - All work of a solver is issued on its stream (lbm_set_stream); functions returning host
  *     data synchronise that stream.
+ *   - Host buffers that kernels can address (pinned / registered memory) are read and written by
+ *     the library's kernels (state upload, moments, populations); other host buffers are staged
+ *     through device memory with copies. Results are the same either way.
  */
 #ifndef LBM_B200_H
 #define LBM_B200_H
