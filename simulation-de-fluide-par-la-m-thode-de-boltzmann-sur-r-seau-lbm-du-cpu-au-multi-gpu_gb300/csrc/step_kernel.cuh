@@ -38,6 +38,12 @@ struct StepArgs {
   const uint32_t* step_ctr;  // lattice steps taken before this launch sequence (device counter)
   uint32_t step_off;         // index of this launch in the sequence
   long long key_base;        // cell offset of this grid in the rounding hash (batched instances)
+  // Strip engine (kernels built with kHalo): the step also writes the populations leaving the
+  // strip through its top owned row (c_y = +1: 2, 5, 6) into ghost row 0 of the strip above, and
+  // those leaving through its bottom owned row (c_y = -1: 4, 7, 8) into ghost row n + 1 of the
+  // strip below. halo[0..3]: offset of that ghost row of the strip above from dst, its plane
+  // stride, the same for the strip below (read only when a boundary row is stored).
+  const long long* halo;
 };
 
 // Stochastic-rounding key of the step a launch performs (16-bit forms): the step index comes

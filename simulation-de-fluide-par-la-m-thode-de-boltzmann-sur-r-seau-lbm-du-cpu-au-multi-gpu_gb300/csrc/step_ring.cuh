@@ -65,7 +65,8 @@ __device__ __forceinline__ int wrap_dir(int j) {
 // sm: 3 staged mask rows (y - 1, y, y + 1) whose word 0 is word tx0 / 32; wr: wrap blocks.
 // kWrapInRow: the stage holds the cell's whole row (columns 0 .. nx - 1 at lx - x ..), and the
 // periodic neighbours of x = 0 and x = nx - 1 are read from it instead of from wrap blocks.
-template <class ST, class A, bool kOpen, class S, bool kWrapInRow = false>
+// kHalo: the strip engine's fused halo (StepArgs::halo_top / halo_bot).
+template <class ST, class A, bool kOpen, class S, bool kWrapInRow = false, bool kHalo = false>
 __device__ __forceinline__ void ring_cell(const StepArgs<ST, ExactPhys<A>>& p, const ST* st,
                                           const uint32_t* sm, const ST* wr, int y, int ym, int yp,
                                           int x, int lx, int word, int lane, bool solids) {
@@ -140,6 +141,22 @@ __device__ __forceinline__ void ring_cell(const StepArgs<ST, ExactPhys<A>>& p, c
   ST* d = p.dst + static_cast<long long>(y) * p.g.pitch + x;
 #pragma unroll
   for (int i = 0; i < kQ; ++i) d[i * plane] = out[i];
+  if constexpr (kHalo) {
+    if (y == p.g.ny - 2) {
+      const long long pl = p.halo[1];
+      ST* h = p.dst + p.halo[0] + x;
+      h[2 * pl] = out[2];
+      h[5 * pl] = out[5];
+      h[6 * pl] = out[6];
+    }
+    if (y == 1) {
+      const long long pl = p.halo[3];
+      ST* h = p.dst + p.halo[2] + x;
+      h[4 * pl] = out[4];
+      h[7 * pl] = out[7];
+      h[8 * pl] = out[8];
+    }
+  }
 }
 
 // 16-bit storage: widen a packed pair of stored (scaled) values to FP32, element 0 in the low
@@ -160,9 +177,9 @@ __device__ __forceinline__ float2 widen_pair<__nv_bfloat16>(uint32_t raw) {
 }
 
 // One pair of cells x, x + 1 (x even) of a strip, 16-bit storage, FP32 fast collision. Same
-// stage layout (and kWrapInRow) as ring_cell; word / lane locate the pair's mask bits (cells
-// x - 1 .. x + 2).
-template <class ST, bool kOpen, class S, bool kWrapInRow = false>
+// stage layout (and kWrapInRow, kHalo) as ring_cell; word / lane locate the pair's mask bits
+// (cells x - 1 .. x + 2).
+template <class ST, bool kOpen, class S, bool kWrapInRow = false, bool kHalo = false>
 __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const ST* st,
                                           const uint32_t* sm, const ST* wr, int y, int x, int lx,
                                           int word, int lane, bool solids) {
@@ -259,8 +276,28 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
   collide_fast_t<FastF32x2>(v, p.k, out);
   const uint32_t ph = sr_pair_hash(p.key_base + row + x, step_rkey(p));
   uint32_t* d = reinterpret_cast<uint32_t*>(p.dst + row + x);
+  uint32_t w[kQ];
 #pragma unroll
-  for (int i = 0; i < kQ; ++i) d[i * (plane / 2)] = encode_pair_sr<ST>(out[i].x, out[i].y, i, ph);
+  for (int i = 0; i < kQ; ++i) {
+    w[i] = encode_pair_sr<ST>(out[i].x, out[i].y, i, ph);
+    d[i * (plane / 2)] = w[i];
+  }
+  if constexpr (kHalo) {
+    if (y == p.g.ny - 2) {
+      const long long pl = p.halo[1] / 2;
+      uint32_t* h = reinterpret_cast<uint32_t*>(p.dst + p.halo[0] + x);
+      h[2 * pl] = w[2];
+      h[5 * pl] = w[5];
+      h[6 * pl] = w[6];
+    }
+    if (y == 1) {
+      const long long pl = p.halo[3] / 2;
+      uint32_t* h = reinterpret_cast<uint32_t*>(p.dst + p.halo[2] + x);
+      h[4 * pl] = w[4];
+      h[7 * pl] = w[7];
+      h[8 * pl] = w[8];
+    }
+  }
 }
 
 // Producer work of one tile (row y, first cell tx0) of grid p into the stage at `base`: arms the
@@ -309,7 +346,7 @@ __device__ __forceinline__ void ring_issue_tile(const StepArgs<ST, Phys>& p, uns
 }
 
 // Consumer work of one tile: warp cw's strip of the stage at `base`.
-template <class ST, class Phys, bool kOpen, class S, int kC>
+template <class ST, class Phys, bool kOpen, class S, int kC, bool kHalo = false>
 __device__ __forceinline__ void ring_consume_tile(const StepArgs<ST, Phys>& p, const unsigned char* base,
                                                   int y, int tx0, int cw, int lane) {
   const int nx = p.g.nx, ny = p.g.ny;
@@ -330,9 +367,9 @@ __device__ __forceinline__ void ring_consume_tile(const StepArgs<ST, Phys>& p, c
     const int x = xw + 32 * S::LC * c + S::LC * lane;
     if (x < nx) {
       if constexpr (S::LC == 2)
-        ring_pair<ST, kOpen, S>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids);
+        ring_pair<ST, kOpen, S, false, kHalo>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids);
       else
-        ring_cell<ST, typename Phys::Arith, kOpen, S>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H, w0 + c,
+        ring_cell<ST, typename Phys::Arith, kOpen, S, false, kHalo>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H, w0 + c,
                                                      lane, solids);
     }
   }
@@ -424,7 +461,7 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
 // grid, row and first cell of a tile; GridTiles below for the solver and the strip engine).
 // The batched ensemble and the adjoint use tile_pipeline with their own stage policies
 // (batch.cu, adjoint.cu).
-template <class ST, class Phys, bool kOpen, int kW, int kC, class Tiles>
+template <class ST, class Phys, bool kOpen, int kW, int kC, class Tiles, bool kHalo = false>
 struct StepPolicy {
   using S = RingShape<ST, kW, kC>;
   static constexpr bool kFinish = false;
@@ -436,16 +473,16 @@ struct StepPolicy {
   }
   __device__ __forceinline__ void consume(int tile, const unsigned char* base, int cw, int lane) const {
     tiles_of.visit(tile, [&](const StepArgs<ST, Phys>& p, int y, int tx0) {
-      ring_consume_tile<ST, Phys, kOpen, S, kC>(p, base, y, tx0, cw, lane);
+      ring_consume_tile<ST, Phys, kOpen, S, kC, kHalo>(p, base, y, tx0, cw, lane);
     });
   }
   __device__ __forceinline__ void finish(int, int) const {}
 };
 
-template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, class Tiles>
+template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, class Tiles, bool kHalo = false>
 __device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& tiles_of, int tiles, int* err) {
   using S = RingShape<ST, kW, kC>;
-  StepPolicy<ST, Phys, kOpen, kW, kC, Tiles> pol{tiles_of};
+  StepPolicy<ST, Phys, kOpen, kW, kC, Tiles, kHalo> pol{tiles_of};
   tile_pipeline<kW, kStages, S::kStageBytes>(smem, pol, tiles, err);
 }
 

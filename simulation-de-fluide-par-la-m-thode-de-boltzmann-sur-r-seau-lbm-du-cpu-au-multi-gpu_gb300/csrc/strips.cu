@@ -9,11 +9,13 @@
 //     row n_k + 1 being the ghost copies of global rows y0 - 1 and y0 + n_k (periodic ring);
 //   * one step = one launch of the ring step kernel over the owned rows of every strip (rows
 //     1 .. n_k, whose y-neighbours are all local; a tile finds its strip by binary search over
-//     the strips' first tiles), then one halo launch for all strips: the ghost row below
+//     the strips' first tiles), with the halo exchange fused into it: the ghost row below
 //     strip k receives the populations moving up (c_y = +1: 2, 5, 6) of the top owned row of the
 //     strip below, the ghost row above receives those moving down (c_y = -1: 4, 7, 8) of the
 //     bottom owned row of the strip above: 3 * nx values per message, the reference's halo
-//     content (engine.hpp:14-20); other ghost-row values are never read;
+//     content (engine.hpp:14-20), written by the step kernel as it stores those rows (one
+//     device, so a neighbour's ghost row is plain memory); other ghost-row values are never
+//     read. A separate halo kernel fills the ghost rows after a state upload;
 //   * every cell update is the solver's, so the result is bit-for-bit that of the undivided
 //     solver (and of the reference's v0) for any number of strips, and the 16-bit forms draw the
 //     same rounding bits (the strip's rows carry their global cell offsets in the hash);
@@ -52,9 +54,12 @@ struct StripView {
 };
 
 // A strip as the step kernel sees it: offsets of its planes and mask rows, its rounding-key
-// base (cell offset of global row y0 - 1), owned rows and first tile of the step's tile index.
+// base (cell offset of global row y0 - 1), owned rows and first tile of the step's tile index,
+// and the fused halo's targets (StepArgs::halo): ghost row 0 of the strip above and ghost row
+// n + 1 of the strip below, as offsets from this strip's planes, with their plane strides.
 struct StripTile {
   long long off, plane, key_base, moff;
+  long long halo[4];
   int n, tile0;
 };
 constexpr int kStripTableSmem = 256;  // strip tables up to this size are staged in shared memory
@@ -84,6 +89,7 @@ struct StripTiles {
     p.g.ny = t.n + 2;
     p.g.plane = t.plane;
     p.key_base = t.key_base;
+    p.halo = t.halo;
     const int local = tile - t.tile0;
     const int r = local / tpr;
     f(p, r + 1, (local - r * tpr) * kTW);
@@ -91,7 +97,8 @@ struct StripTiles {
 };
 
 // One step of every strip: the solver's ring kernel (8 consumer warps x 2 passes, 2 stages)
-// over the strips' tiles.
+// over the strips' tiles, with the halo exchange fused into the stores of each strip's top and
+// bottom owned rows (the ghost rows of the destination buffer are complete when it ends).
 template <class ST, class Phys, bool kOpen, int kMinBlocks>
 __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips, int tpr,
@@ -106,8 +113,9 @@ __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     __syncthreads();
     t = s_tab;
   }
-  const StripTiles<ST, Phys, S::TW> tiles_of{base, t, strips, tpr};
-  ring_pipeline<ST, Phys, kOpen, 8, 2, 2>(smem, tiles_of, tiles, err);
+  using Tiles = StripTiles<ST, Phys, S::TW>;
+  const Tiles tiles_of{base, t, strips, tpr};
+  ring_pipeline<ST, Phys, kOpen, 8, 2, 2, Tiles, true>(smem, tiles_of, tiles, err);
 }
 
 // Device halo exchange of all strips (raw elements E, the storage bits): thread per
@@ -222,13 +230,13 @@ int halo_t(lbm_strips* h, int b) {
   return LBM_OK;
 }
 
-// `steps` steps: per step, one ring launch over every strip's owned rows, then the halo
-// exchange into the state just written; then the step counter advances.
+// `steps` steps: one ring launch per step over every strip's owned rows (halo fused); then the
+// step counter advances.
 template <class ST, bool kOpen>
 int steps_t(lbm_strips* h, int steps) {
   using Phys = typename Form<ST>::Phys;
   using T = typename StoreTraits<ST>::T;
-  constexpr int kMin = sizeof(ST) == 2 ? 3 : 1;  // as the solver's variants 17 / 12
+  constexpr int kMin = sizeof(ST) == 8 ? 1 : 3;  // 3 resident blocks (72 registers) but in FP64
   using S = RingShape<ST, 8, 2>;
   const auto kernel = strip_ring_kernel<ST, Phys, kOpen, kMin>;
   const size_t smem = ring_smem_bytes<S>(2) +
@@ -254,7 +262,6 @@ int steps_t(lbm_strips* h, int steps) {
     a.step_off = static_cast<uint32_t>(s);
     S_CUDA(h, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, h->stream, a,
                                static_cast<const StripTile*>(h->tiles_d), h->strips, tpr, tiles, err));
-    if (int rc = halo_t<ST>(h, h->cur ^ 1)) return rc;
     h->cur ^= 1;
   }
   counter_add_kernel<<<1, 1, 0, h->stream>>>(h->ctr, static_cast<uint32_t>(steps));
@@ -519,8 +526,18 @@ int lbm_strips_create(int nx, int ny, const uint8_t* solid, double tau, double f
     std::vector<StripTile> tt(strips);
     int tile0 = 0;
     for (int k = 0; k < strips; ++k) {
-      tt[k] = StripTile{h->off[k], views[k].plane, static_cast<long long>(h->y0[k] - 1) * h->pitch, h->moff[k],
-                        h->n[k], tile0};
+      const int up = k == strips - 1 ? 0 : k + 1, dn = k == 0 ? strips - 1 : k - 1;
+      StripTile& t = tt[k];
+      t.off = h->off[k];
+      t.plane = views[k].plane;
+      t.key_base = static_cast<long long>(h->y0[k] - 1) * h->pitch;
+      t.moff = h->moff[k];
+      t.halo[0] = h->off[up] - h->off[k];  // ghost row 0 of the strip above
+      t.halo[1] = views[up].plane;
+      t.halo[2] = h->off[dn] + static_cast<long long>(h->n[dn] + 1) * h->pitch - h->off[k];  // row n + 1 below
+      t.halo[3] = views[dn].plane;
+      t.n = h->n[k];
+      t.tile0 = tile0;
       tile0 += tpr * h->n[k];
     }
     if (e == cudaSuccess) e = cudaMalloc(&h->tiles_d, strips * sizeof(StripTile));
