@@ -220,8 +220,10 @@ int launch_ring_t(lbm_solver* s, int steps) {
       a.dst = static_cast<ST*>(s->buf[s->cur ^ 1]);
       a.step_ctr = s->step_ctr;
       a.step_off = static_cast<uint32_t>(k);
+      // Odd steps (by buffer parity) walk the tiles backwards: they start on the rows the
+      // previous step wrote last.
       LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, s->stream, a, tpr, tiles, 0,
-                                   s->err_flag));
+                                   s->cur, s->err_flag));
       s->cur ^= 1;
     }
     LBM_CUDA(s, cudaGetLastError());
