@@ -107,11 +107,14 @@ struct AdjTiles {
 struct TilePos {
   int b, y, ym, yp, tx0;
 };
+// reverse: the tile order is mirrored (alternate steps start on the rows the previous step
+// wrote last, still in L2).
 template <int kTW>
-__device__ __forceinline__ TilePos tile_pos(const AdjGeom& g, const AdjTiles& at, int tile) {
+__device__ __forceinline__ TilePos tile_pos(const AdjGeom& g, const AdjTiles& at, int tile, int reverse) {
   const uint32_t i = at.grid.div(static_cast<uint32_t>(tile));
   const uint32_t k = static_cast<uint32_t>(tile) - i * at.grid.d;
-  const uint32_t lin = k * static_cast<uint32_t>(at.q) + min(k, static_cast<uint32_t>(at.r)) + i;
+  uint32_t lin = k * static_cast<uint32_t>(at.q) + min(k, static_cast<uint32_t>(at.r)) + i;
+  if (reverse) lin = static_cast<uint32_t>(at.total) - 1u - lin;
   TilePos t;
   t.b = static_cast<int>(at.per_inst.div(lin));
   const uint32_t r = lin - static_cast<uint32_t>(t.b) * at.per_inst.d;
@@ -132,6 +135,7 @@ struct FwdArgs {
   AdjTiles at;
   CollideConsts<T> k;      // the collision's constants (cf_* unused: the force is per cell)
   double* obj;             // per-warp slots [instance][block][warp] accumulating sum u_x, or null
+  int reverse;             // walk the tiles from the last (alternate steps)
 };
 
 template <class T>
@@ -148,6 +152,7 @@ struct BwdArgs {
   T omega, fp, fx, fy, hfx, hfy, obj_coef;
   int flush;
   double* grads;           // per-warp slots [instance][block][warp][omega_bar, fx_bar, fy_bar]
+  int reverse;             // walk the tiles from the last (alternate steps)
 };
 
 // Row of plane j staged for the transpose gather: the source c + e_j lies in row y + c_y.
@@ -296,7 +301,7 @@ struct AdjForward {
 
   __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full) const {
     const AdjGeom& g = p.g;
-    const TilePos t = tile_pos<S::TW>(g, p.at, tile);
+    const TilePos t = tile_pos<S::TW>(g, p.at, tile, p.reverse);
     const RowSpan<S> rs(g, t.tx0, sizeof(T));
     const bool lo = t.tx0 == 0, hi = t.tx0 + S::TW >= g.nx;
     const uint32_t fb = p.alpha ? field_bytes<S>(g, t.tx0, sizeof(T)) : 0u;
@@ -349,7 +354,7 @@ struct AdjForward {
 
   __device__ __forceinline__ void consume(int tile, const unsigned char* base, int cw, int lane) {
     const AdjGeom& g = p.g;
-    const TilePos t = tile_pos<S::TW>(g, p.at, tile);
+    const TilePos t = tile_pos<S::TW>(g, p.at, tile, p.reverse);
     if (t.b != cur_b) {
       flush(cw, lane);
       cur_b = t.b;
@@ -479,7 +484,7 @@ struct AdjBackward {
 
   __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full) const {
     const AdjGeom& g = p.g;
-    const TilePos t = tile_pos<S::TW>(g, p.at, tile);
+    const TilePos t = tile_pos<S::TW>(g, p.at, tile, p.reverse);
     const RowSpan<S> rs(g, t.tx0, sizeof(T));
     const bool lo = t.tx0 == 0, hi = t.tx0 + S::TW >= g.nx;
     const bool z = p.Z != nullptr;
@@ -596,7 +601,7 @@ struct AdjBackward {
 
   __device__ __forceinline__ void consume(int tile, const unsigned char* base, int cw, int lane) {
     const AdjGeom& g = p.g;
-    const TilePos t = tile_pos<S::TW>(g, p.at, tile);
+    const TilePos t = tile_pos<S::TW>(g, p.at, tile, p.reverse);
     if (t.b != cur_b) {
       flush(cw, lane);
       cur_b = t.b;
@@ -901,11 +906,12 @@ int launch_ring(lbm_adjoint* a, K kernel, int grid, size_t smem, const Args& p) 
 }
 
 template <class A>
-int launch_forward(lbm_adjoint* a, FwdArgs<typename A::T> p, const void* R, void* Rn, double* obj) {
+int launch_forward(lbm_adjoint* a, FwdArgs<typename A::T> p, const void* R, void* Rn, double* obj, int reverse) {
   using T = typename A::T;
   p.R = static_cast<const T*>(R);
   p.Rn = static_cast<T*>(Rn);
   p.obj = obj;
+  p.reverse = reverse;
   return with_shape<T>(a->fwd_c, [&](auto kc) {
     constexpr int kC = decltype(kc)::value;
     return launch_ring(a, AdjKernels<A, kC>::fwd, a->fwd_grid, AdjLaunch<T, kC>::fwd_smem(), p);
@@ -977,12 +983,12 @@ int forward_t(lbm_adjoint* a, const void* s0_host, int steps, int window, double
     const bool in_window = t >= steps - window + 1;
     const bool is_ckpt = (t + 1) % a->K == 0;
     void* out = is_ckpt ? ckpt + static_cast<size_t>((t + 1) / a->K) * sb : a->state[spare];
-    if (const int rc = launch_forward<A>(a, p, cur, out, in_window ? a->obj_part : nullptr)) return rc;
+    if (const int rc = launch_forward<A>(a, p, cur, out, in_window ? a->obj_part : nullptr, t & 1)) return rc;
     if (!is_ckpt) spare ^= 1;
     cur = out;
   }
   ADJ_CUDA(a, cudaEventRecord(a->ev[1], a->stream));
-  if (const int rc = launch_forward<A>(a, p, cur, nullptr, a->obj_part)) return rc;  // final state's objective
+  if (const int rc = launch_forward<A>(a, p, cur, nullptr, a->obj_part, steps & 1)) return rc;  // final state's objective
   ADJ_CUDA(a, cudaGetLastError());
   std::vector<double> sums;
   if (const int rc = read_sums(a, a->obj_part, a->fwd_grid, 1, sums)) return rc;
@@ -1045,7 +1051,8 @@ int backward_t(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* d
     const char* base = static_cast<const char*>(a->ckpt) + static_cast<size_t>(s) * sb;
     auto state_at = [&](int t) -> const void* { return t == t0 ? base : seg + static_cast<size_t>(t - t0 - 1) * sb; };
     for (int t = t0; t < t1; ++t)
-      if (const int rc = launch_forward<A>(a, pf, state_at(t), seg + static_cast<size_t>(t - t0) * sb, nullptr)) return rc;
+      if (const int rc = launch_forward<A>(a, pf, state_at(t), seg + static_cast<size_t>(t - t0) * sb, nullptr, t & 1))
+        return rc;
     // Adjoint steps t1 (only for the last segment: the final state) .. t0.
     const int top = (s == nseg - 1) ? t1 : t1 - 1;
     for (int t = top; t >= t0; --t) {
@@ -1055,6 +1062,7 @@ int backward_t(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* d
       pb.Yb = static_cast<T*>(a->ybar[yb]);
       pb.obj_coef = in_window ? coef : T(0);
       pb.flush = t == t0 ? 1 : 0;
+      pb.reverse = t & 1;
       if (const int rc = launch_backward<A>(a, pb)) return rc;
       first = false;
       yb ^= 1;

@@ -75,7 +75,8 @@ struct BatchArgs {
   PlaneScales sc;
   const uint32_t* step;  // lattice steps taken (device counter; stochastic-rounding key)
   const StagedArgs<ST, Phys>* args;  // [instance][parity]
-  int parity;                        // src == buffer `parity`
+  int parity;                        // src == buffer `parity`; odd parity walks the tiles backwards
+  int tiles;                         // ring tiles of the ensemble
 };
 
 // Device step counter of a batch: read by every step launch, advanced by one after it (inside a
@@ -298,6 +299,9 @@ struct BatchFlatPolicy {
   // between them (strip tiles: 18 per segment, those that apply; whole-row tiles: at most
   // 2 per plane and one per mask row) and lane 0 the step arguments' copy.
   __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
+    // Odd steps walk the tiles from the last: they start on the rows the previous step wrote
+    // last, still in L2 (the consumers only read what the producer staged).
+    if (a.parity) tile = a.tiles - 1 - tile;
     const int k = instance_of(tile);
     const Inst& d = a.inst[k];
     const StepArgs<ST, Phys> p = grid_of(d);
@@ -653,6 +657,7 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
   a.sc = b->sc;
   a.step = b->step_d;
   a.args = static_cast<const StagedArgs<ST, Phys>*>(b->args_d);
+  a.tiles = b->tiles;
   int* err = reinterpret_cast<int*>(b->step_d + 1);
   for (int s = 0; s < steps; ++s) {
     a.src = static_cast<const ST*>(b->buf[b->cur]);

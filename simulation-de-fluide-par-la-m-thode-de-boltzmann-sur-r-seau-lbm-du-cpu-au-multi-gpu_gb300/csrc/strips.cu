@@ -70,9 +70,10 @@ template <class ST, class Phys, int kTW>
 struct StripTiles {
   const StepArgs<ST, Phys>& base;  // src / dst / mask: buffer bases; g: nx, pitch, mask words
   const StripTile* tab;
-  int strips, tpr;
+  int strips, tpr, tiles, reverse;  // reverse: walk the tiles from the last (alternate steps)
   template <class F>
   __device__ __forceinline__ void visit(int tile, F&& f) const {
+    if (reverse) tile = tiles - 1 - tile;
     int lo = 0, hi = strips - 1;
     while (lo < hi) {
       const int mid = (lo + hi + 1) >> 1;
@@ -102,7 +103,7 @@ struct StripTiles {
 template <class ST, class Phys, bool kOpen, int kMinBlocks>
 __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips, int tpr,
-                      int tiles, int* err) {
+                      int tiles, int reverse, int* err) {
   using S = RingShape<ST, 8, 2>;
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
@@ -114,7 +115,7 @@ __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     t = s_tab;
   }
   using Tiles = StripTiles<ST, Phys, S::TW>;
-  const Tiles tiles_of{base, t, strips, tpr};
+  const Tiles tiles_of{base, t, strips, tpr, tiles, reverse};
   ring_pipeline<ST, Phys, kOpen, 8, 2, 2, Tiles, true>(smem, tiles_of, tiles, err);
 }
 
@@ -261,7 +262,7 @@ int steps_t(lbm_strips* h, int steps) {
     a.dst = static_cast<ST*>(h->buf[h->cur ^ 1]);
     a.step_off = static_cast<uint32_t>(s);
     S_CUDA(h, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, h->stream, a,
-                               static_cast<const StripTile*>(h->tiles_d), h->strips, tpr, tiles, err));
+                               static_cast<const StripTile*>(h->tiles_d), h->strips, tpr, tiles, h->cur, err));
     h->cur ^= 1;
   }
   counter_add_kernel<<<1, 1, 0, h->stream>>>(h->ctr, static_cast<uint32_t>(steps));
