@@ -177,11 +177,13 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * 2 passes per strip, 2 stages; 13 = the same with 3 stages; 14 = 12 capped at 56 registers for
  * 4 resident blocks; 15 = 4 consumer warps, 3 stages; 16 = 15 capped for 7 resident blocks;
  * 17 = 12 capped for 3 resident blocks; 18 = 17 with 3 stages; 19 = 17 with 1 pass per strip
- * (half-width tiles) and 4 stages. The ring variants are launched with programmatic stream
+ * (half-width tiles) and 4 stages; 20 = 8 consumer warps, 4 passes per strip (double-width
+ * tiles), 2 stages, 2 resident blocks; 21 = 4 consumer warps, 4 passes, 2 stages, 5 blocks. The ring variants are launched with programmatic stream
  * serialisation (the next step's blocks are scheduled while the previous step drains).
  * -1 (the default), by grid size from a sweep on GB300: rows narrower than 256 cells: 0; plain
- * FP32: 19 below 2^17 cells, 17 below 2^21, 12 above; 16-bit storage: 19 below 2^21 cells, 17
- * above; FP64: 12 with at least two 512-cell tiles per SM, 0 otherwise.
+ * FP32: 19 below 2^17 cells, 17 below 2^21, 12 above; 16-bit storage: 19 below 2^21 cells, 20
+ * with rows of at least 2048 cells and at least 2^22 cells, 17 otherwise; FP64: 12 with at least
+ * two 512-cell tiles per SM, 0 otherwise.
  * The 16-bit forms round stored populations stochastically (see lbm_create); every variant
  * derives the same random bits, so the variants give the same results. */
 int lbm_set_variant(lbm_solver* s, int variant);

@@ -234,8 +234,9 @@ int launch_ring_t(lbm_solver* s, int steps) {
 // Automatic kernel choice (variant < 0), from a sweep of every variant on one GB300 (channel,
 // best of 3 runs, MLUPS): plain FP32: 256^2 v19 20.8k (v0 19.8k), 512^2 / 1024x256 v17 51.9k /
 // 51.7k (v12 47.4k / 46.2k), 1024^2 v17 83.9k (v12 81.7k), 2048^2 v12 86.2k, 4096^2 v12 90.6k;
-// 16-bit storage: 256^2 v19 20.2k (v0 13.5k), 512^2 v19 61.2k, 1024^2 v19 114.4k (v17 109.6k),
-// 2048^2 v17 138.3k (v14 142.7k), 4096^2 v17 158.2k. Rows narrower than 256 cells take the
+// 16-bit storage: 256^2 v19 20.2k (v0 13.5k), 512^2 v19 61.2k, 1024^2 v19 114.5k (v17 108.6k,
+// v20 91.1k: its 2048-cell tiles are half empty on 1024-cell rows), 2048^2 v20 157.1k (v17
+// 143.0k), 4096^2 v20 168.7k (v17 159.3k). Rows narrower than 256 cells take the
 // direct kernel (0), whose 128-cell chunks leave fewer lanes idle than the rings' wide tiles
 // (FP64 on 100 x 2000: the ring 12 reached 1.0k MLUPS with a fifth of its lanes busy); otherwise
 // FP64 (FP64-ALU-bound) takes the ring 12 with at least two of its tiles per SM, else 0.
@@ -248,7 +249,10 @@ int auto_variant(const lbm_solver* s) {
     const long long tiles = static_cast<long long>((s->nx + S::TW - 1) / S::TW) * s->ny;
     return tiles < 2LL * s->sm_count ? 0 : 12;
   }
-  if (sizeof(ST) == 2) return cells < (2LL << 20) ? 19 : 17;
+  if (sizeof(ST) == 2) {
+    if (cells < (2LL << 20)) return 19;
+    return (s->nx >= 2048 && cells >= (4LL << 20)) ? 20 : 17;  // 2048-cell tiles need wide rows
+  }
   return cells < (1LL << 17) ? 19 : (cells < (2LL << 20) ? 17 : 12);
 }
 
@@ -275,6 +279,8 @@ int launch_steps_o(lbm_solver* s, int steps) {
     case 17: return launch_ring_t<ST, kOpen, 8, 2, 2, 3>(s, steps);
     case 18: return launch_ring_t<ST, kOpen, 8, 2, 3, 3>(s, steps);
     case 19: return launch_ring_t<ST, kOpen, 8, 1, 4, 3>(s, steps);
+    case 20: return launch_ring_t<ST, kOpen, 8, 4, 2, 2>(s, steps);
+    case 21: return launch_ring_t<ST, kOpen, 4, 4, 2, 5>(s, steps);
     default: return launch_steps_t<ST, kOpen, 0>(s, steps);
   }
 }
@@ -920,7 +926,7 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
 
 int lbm_set_variant(lbm_solver* s, int variant) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
-  if (variant < -1 || variant > 19)
+  if (variant < -1 || variant > 21)
     return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 17]");
   s->variant = variant;
   lbm_b200::drop_step_graph(s);
