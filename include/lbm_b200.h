@@ -178,7 +178,8 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * 4 resident blocks; 15 = 4 consumer warps, 3 stages; 16 = 15 capped for 7 resident blocks;
  * 17 = 12 capped for 3 resident blocks; 18 = 17 with 3 stages; 19 = 17 with 1 pass per strip
  * (half-width tiles) and 4 stages; 20 = 8 consumer warps, 4 passes per strip (double-width
- * tiles), 2 stages, 2 resident blocks; 21 = 4 consumer warps, 4 passes, 2 stages, 5 blocks. The ring variants are launched with programmatic stream
+ * tiles), 2 stages, 2 resident blocks; 21 = 4 consumer warps, 4 passes, 2 stages, 5 blocks;
+ * 22 = 20 with 3 stages. The ring variants are launched with programmatic stream
  * serialisation (the next step's blocks are scheduled while the previous step drains).
  * -1 (the default), by grid size from a sweep on GB300: rows narrower than 256 cells: 0; plain
  * FP32: 19 below 2^17 cells, 17 below 2^21, 12 above; 16-bit storage: 19 below 2^21 cells, 20

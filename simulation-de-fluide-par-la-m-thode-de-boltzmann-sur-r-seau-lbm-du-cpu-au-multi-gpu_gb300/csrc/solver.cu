@@ -281,6 +281,7 @@ int launch_steps_o(lbm_solver* s, int steps) {
     case 19: return launch_ring_t<ST, kOpen, 8, 1, 4, 3>(s, steps);
     case 20: return launch_ring_t<ST, kOpen, 8, 4, 2, 2>(s, steps);
     case 21: return launch_ring_t<ST, kOpen, 4, 4, 2, 5>(s, steps);
+    case 22: return launch_ring_t<ST, kOpen, 8, 4, 3, 2>(s, steps);
     default: return launch_steps_t<ST, kOpen, 0>(s, steps);
   }
 }
@@ -926,7 +927,7 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
 
 int lbm_set_variant(lbm_solver* s, int variant) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
-  if (variant < -1 || variant > 21)
+  if (variant < -1 || variant > 22)
     return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 17]");
   s->variant = variant;
   lbm_b200::drop_step_graph(s);

@@ -18,7 +18,7 @@ from conftest import golden_cases, initial_state, load_golden
 pytestmark = pytest.mark.gpu
 
 FORMS = ["fp16", "bf16"]
-VARIANTS = list(range(22))
+VARIANTS = list(range(23))
 VELOCITY_L2_MAX = {"fp16": 1e-3, "bf16": 1e-2}
 
 

@@ -132,7 +132,7 @@ def test_divergence_is_detected(gpu_lib):
         assert not s.check_finite()
 
 
-VARIANTS = list(range(22))
+VARIANTS = list(range(23))
 
 
 @pytest.mark.parametrize("variant", VARIANTS)
