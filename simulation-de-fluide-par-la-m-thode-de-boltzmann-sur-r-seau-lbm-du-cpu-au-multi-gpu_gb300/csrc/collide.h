@@ -137,7 +137,7 @@ LBM_HD void collide_exact_post(const typename A::T (&g)[kQ], typename A::T omega
 
   T geq[kQ];
   geq[0] = A::mul(A::k(weight<S>(0)), A::sub(drho, A::mul(rho, s15)));
-#if defined(__CUDACC__)
+#if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
   for (int i = 1; i < kQ; ++i) geq[i] = A::mul(A::k(weight<S>(i)), A::add(drho, A::mul(rho, bracket[i])));
@@ -174,7 +174,7 @@ LBM_HD void collide_exact_post(const typename A::T (&g)[kQ], typename A::T omega
   guo[6] = A::mul(A::k(weight<S>(6)), A::add(A::mul(three, t[6]), pq));
   guo[8] = A::mul(A::k(weight<S>(8)), A::add(A::mul(three, t[8]), pq));
 
-#if defined(__CUDACC__)
+#if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
   for (int i = 0; i < kQ; ++i)
@@ -230,7 +230,7 @@ LBM_HD void moments_exact(const typename A::T (&g)[kQ], typename A::T hfx, typen
   using T = typename A::T;
   using S = typename A::S;
   T m0 = g[0];
-#if defined(__CUDACC__)
+#if defined(__CUDA_ARCH__)
 #pragma unroll
 #endif
   for (int i = 1; i < kQ; ++i) m0 = A::add(m0, g[i]);
