@@ -276,7 +276,7 @@ def wake_report(pkg):
     return out
 
 
-def batch_report(pkg, peak):
+def batch_report(pkg, peak, autotune=True):
     """Batched ensemble: 256 uneven closed channels (nx ~ U[64,1024], ny ~ U[32,512], 1-4 discs,
     tau ~ U[0.52,1], fx ~ U[1e-6,1e-5], seed 7), autotuned, 640 steps as CUDA graphs of one
     persistent launch per step, against the same instances stepped one launch per instance."""
@@ -287,7 +287,7 @@ def batch_report(pkg, peak):
         try:
             with pkg.Batch(specs, precision=prec) as b:
                 b.init_equilibrium(1.0, 0.0, 0.0)
-                tune = b.autotune()
+                tune = b.autotune() if autotune else "default: ring 8x2 stages=2 (not tuned)"
                 b.run(64)
                 tb = b.timed_run(640)
                 ts = b.run_separate(64)
@@ -438,7 +438,7 @@ def run_ours(args):
         if args.adjoint:
             forms["adjoint"] = adjoint_report(pkg, peak)
         if args.batch:
-            forms["batch"] = batch_report(pkg, peak)
+            forms["batch"] = batch_report(pkg, peak, args.batch_autotune)
         if args.scale:
             forms["scale"] = scale_report(pkg, peak)
         if args.wake:
@@ -557,6 +557,8 @@ def main():
                     help="skip the adjoint form")
     ap.add_argument("--no-batch", dest="batch", action="store_false",
                     help="skip the batched ensemble form")
+    ap.add_argument("--no-batch-autotune", dest="batch_autotune", action="store_false",
+                    help="batched ensemble with the library's default launch (profiling)")
     ap.add_argument("--no-scale", dest="scale", action="store_false",
                     help="skip the 2048^2 / 4096^2 / 8192^2 FP32 and FP64 scale report")
     ap.add_argument("--no-wake", dest="wake", action="store_false",
