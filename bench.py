@@ -204,11 +204,27 @@ def cpu_baseline(orc, n: int, budget_s: float = 8.0):
     t0 = time.perf_counter()
     bufs.run(TAU, FX, FY, steps, threads=threads)
     dt = time.perf_counter() - t0
+    # The reference's sequential v0 (push, AoS) on one core: a bounded 1024^2 sample.
+    m0 = 1024
+    mask0 = np.zeros(m0 * m0, np.uint8)
+    mask0[:m0] = 1
+    mask0[-m0:] = 1
+    s0 = orc.seeded_state(SEED, AMP, m0, m0, mask0)
+    t0 = time.perf_counter()
+    orc.v0_run(m0, m0, mask0, TAU, FX, FY, s0, 1)
+    one = time.perf_counter() - t0
+    k0 = int(max(1, min(20, 3.0 / max(one, 1e-6))))
+    t0 = time.perf_counter()
+    orc.v0_run(m0, m0, mask0, TAU, FX, FY, s0, k0)
+    v0_mlups = m0 * m0 * k0 / (time.perf_counter() - t0) / 1e6
     return {"value": round(n * n * steps / dt / 1e6, 2), "unit": "MLUPS", "cores": threads,
             "kind": "port",
             "sample": f"{n}x{n} walled channel, {steps} steps after 1 warm-up step, FP32, "
                       f"oracle pull port of reference v1 (src/v1_omp/solver_v1.cpp), "
-                      f"{threads} OpenMP threads"}
+                      f"{threads} OpenMP threads",
+            "v0_single_core": {"value": round(v0_mlups, 2), "unit": "MLUPS", "cores": 1,
+                               "sample": f"{m0}x{m0} walled channel, {k0} steps, FP32, oracle "
+                                         f"restatement of reference v0 (src/v0_cpu/solver_v0.cpp)"}}
 
 
 def accuracy_report(pkg):
