@@ -97,14 +97,14 @@ struct StripTiles {
   }
 };
 
-// One step of every strip: the solver's ring kernel (8 consumer warps x 2 passes, 2 stages)
+// One step of every strip: the solver's ring kernel (8 consumer warps x kC passes, 2 stages)
 // over the strips' tiles, with the halo exchange fused into the stores of each strip's top and
 // bottom owned rows (the ghost rows of the destination buffer are complete when it ends).
-template <class ST, class Phys, bool kOpen, int kMinBlocks>
+template <class ST, class Phys, bool kOpen, int kC, int kMinBlocks>
 __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips, int tpr,
                       int tiles, int reverse, int* err) {
-  using S = RingShape<ST, 8, 2>;
+  using S = RingShape<ST, 8, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
   const StripTile* t = tab;
@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(32 * 9, kMinBlocks)
   }
   using Tiles = StripTiles<ST, Phys, S::TW>;
   const Tiles tiles_of{base, t, strips, tpr, tiles, reverse};
-  ring_pipeline<ST, Phys, kOpen, 8, 2, 2, Tiles, true>(smem, tiles_of, tiles, err);
+  ring_pipeline<ST, Phys, kOpen, 8, kC, 2, Tiles, true>(smem, tiles_of, tiles, err);
 }
 
 // Device halo exchange of all strips (raw elements E, the storage bits): thread per
@@ -171,6 +171,7 @@ struct lbm_strips {
   cudaGraphExec_t graph = nullptr;
   int graph_cur = -1;
   bool graphs = true;
+  int passes = 2;  // ring passes per strip: 4 (2048-cell tiles) for 16-bit storage on rows >= 2048
   int sm_count = 0;
   std::string err;
 };
@@ -232,14 +233,17 @@ int halo_t(lbm_strips* h, int b) {
 }
 
 // `steps` steps: one ring launch per step over every strip's owned rows (halo fused); then the
-// step counter advances.
-template <class ST, bool kOpen>
-int steps_t(lbm_strips* h, int steps) {
+// step counter advances. kC: ring passes per strip (the solver's variant 12 / 17 shape, or
+// variant 20's for 16-bit storage on wide rows).
+template <class ST, bool kOpen, int kC>
+int steps_tc(lbm_strips* h, int steps) {
   using Phys = typename Form<ST>::Phys;
   using T = typename StoreTraits<ST>::T;
-  constexpr int kMin = sizeof(ST) == 8 ? 1 : 3;  // 3 resident blocks (72 registers) but in FP64
-  using S = RingShape<ST, 8, 2>;
-  const auto kernel = strip_ring_kernel<ST, Phys, kOpen, kMin>;
+  // Register caps: 3 resident blocks (72 registers); 2 for the four-pass shape with open x
+  // boundaries (it would spill at 72); none in FP64.
+  constexpr int kMin = sizeof(ST) == 8 ? 1 : ((kC == 4 && kOpen) ? 2 : 3);
+  using S = RingShape<ST, 8, kC>;
+  const auto kernel = strip_ring_kernel<ST, Phys, kOpen, kC, kMin>;
   const size_t smem = ring_smem_bytes<S>(2) +
                       (h->strips <= kStripTableSmem ? h->strips * sizeof(StripTile) : 0);
   S_CUDA(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
@@ -268,6 +272,14 @@ int steps_t(lbm_strips* h, int steps) {
   counter_add_kernel<<<1, 1, 0, h->stream>>>(h->ctr, static_cast<uint32_t>(steps));
   S_CUDA(h, cudaGetLastError());
   return LBM_OK;
+}
+
+template <class ST, bool kOpen>
+int steps_t(lbm_strips* h, int steps) {
+  if constexpr (sizeof(ST) == 2) {
+    if (h->passes == 4) return steps_tc<ST, kOpen, 4>(h, steps);
+  }
+  return steps_tc<ST, kOpen, 2>(h, steps);
 }
 
 template <class ST>
@@ -522,7 +534,8 @@ int lbm_strips_create(int nx, int ny, const uint8_t* solid, double tau, double f
   // The step kernel's strip table: tiles of the ring shape (8 consumer warps x 2 passes: 512
   // cells per tile, 1024 with 16-bit storage) over the owned rows, strip after strip.
   {
-    const int tw = 32 * 8 * 2 * (elem == 2 ? 2 : 1);
+    h->passes = (elem == 2 && nx >= 2048) ? 4 : 2;
+    const int tw = 32 * 8 * h->passes * (elem == 2 ? 2 : 1);
     const int tpr = (nx + tw - 1) / tw;
     std::vector<StripTile> tt(strips);
     int tile0 = 0;

@@ -75,3 +75,23 @@ def test_strips_need_two_rows_each(gpu_lib):
     mask = np.zeros(32 * 9, np.uint8)
     with pytest.raises(ValueError):
         gpu_lib.Strips(32, 9, 0.6, 0.0, 0.0, mask, 5)
+
+
+@pytest.mark.parametrize("precision", ["fp16", "bf16"])
+@pytest.mark.parametrize("open_x", [False, True])
+def test_wide_16bit_strips(gpu_lib, orc, precision, open_x):
+    """Rows of at least 2048 cells with 16-bit storage take 2048-cell tiles (four passes per
+    strip); 2100 cells leave a partial last tile. Same bits as the whole-lattice solver."""
+    nx, ny = 2100, 40
+    mask = gpu_lib.make_channel(nx, ny) | gpu_lib.make_cylinder(nx, ny, 2060.0, 20.5, 11.0)
+    s0 = orc.seeded_state(7, 1e-3, nx, ny, mask, "f32")
+    with gpu_lib.Solver(nx, ny, 0.58, 2e-6, 0.0, mask, precision=precision) as a, \
+            gpu_lib.Strips(nx, ny, 0.58, 2e-6, 0.0, mask, 3, precision=precision) as b:
+        for s in (a, b):
+            if open_x:
+                s.set_inflow_outflow(0.03)
+                s.init_equilibrium(1.0, 0.03, 0.0)
+            else:
+                s.set_populations(s0)
+            s.run(70)
+        assert np.array_equal(a.populations(), b.populations())
