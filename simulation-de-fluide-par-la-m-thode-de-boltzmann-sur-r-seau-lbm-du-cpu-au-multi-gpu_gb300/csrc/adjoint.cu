@@ -50,7 +50,11 @@ using namespace lbm_b200;
 namespace {
 
 constexpr int kAdjW = 8;            // consumer warps per block
-constexpr int kAdjThreads = 32 * (kAdjW + 1);
+// Producer warps per block (tile_pipeline). One: a second one, which speeds up the batched
+// ensemble's many short copies, made both adjoint kernels slower (27.8 -> 28.4 us forward,
+// 72.8 -> 75.6 us backward on the 512 x 128 x 32 benchmark batch).
+constexpr int kAdjProd = 1;
+constexpr int kAdjThreads = 32 * (kAdjW + kAdjProd);
 constexpr int kAuxThreads = 256;    // state conversion, field casts, slot sums
 
 // Geometry shared by all instances. A state is 9 pitched planes; per-cell fields (alpha and its
@@ -378,7 +382,7 @@ __global__ void __launch_bounds__(kAdjThreads, kMinBlocks)
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
   AdjForward<A, kC> pol{p};
-  tile_pipeline<kAdjW, kStages, FwdStage<typename A::T, kC>::kBytes>(smem, pol, p.at.total, err);
+  tile_pipeline<kAdjW, kStages, FwdStage<typename A::T, kC>::kBytes, kAdjProd>(smem, pol, p.at.total, err);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -625,7 +629,7 @@ __global__ void __launch_bounds__(kAdjThreads, kMinBlocks)
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
   AdjBackward<T, kC> pol{p};
-  tile_pipeline<kAdjW, kStages, BwdStage<T, kC>::kBytes>(smem, pol, p.at.total, err);
+  tile_pipeline<kAdjW, kStages, BwdStage<T, kC>::kBytes, kAdjProd>(smem, pol, p.at.total, err);
 }
 
 // Per-instance sums of the per-warp slots (nval values each): block b adds its instance's

@@ -145,7 +145,12 @@ struct FlatShape {
   static constexpr int kMaskBytes = kW * 3 * MW * 4;
   static constexpr int kWrapBytes = kW * 6 * 16;
   static constexpr int kStageBytes = kPlaneBytes + kMaskBytes + kWrapBytes;
-  static constexpr int kThreads = 32 * (kW + 1);
+  // Producer warps of a ring block: two for FP32, whose many short copies per tile make one
+  // producer the limit on uneven ensembles (measured on the 256-channel benchmark ensemble: 59.0k
+  // -> 65.6k MLUPS); one for the 16-bit forms (a tenth warp would cap their registers below what
+  // their collision needs) and for FP64 (FP64-ALU-bound).
+  static constexpr int kProd = sizeof(ST) == 4 ? 2 : 1;
+  static constexpr int kThreads = 32 * (kW + kProd);
   static_assert(SW % 32 == 0 && (SROW * static_cast<int>(sizeof(ST))) % 16 == 0 && kStageBytes % 16 == 0,
                 "stage parts must stay 16-byte aligned");
 };
@@ -426,7 +431,7 @@ constexpr int batch_ring_min_blocks() {
 }
 
 template <class ST, class Phys, int kW, int kC, int kStages>
-__global__ void __launch_bounds__(32 * (kW + 1), (batch_ring_min_blocks<ST, kW>()))
+__global__ void __launch_bounds__(FlatShape<ST, kW, kC>::kThreads, (batch_ring_min_blocks<ST, kW>()))
     batch_ring_kernel(const BatchArgs<ST, Phys> a, int tiles, int* err) {
   using Pol = BatchFlatPolicy<ST, Phys, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -434,7 +439,7 @@ __global__ void __launch_bounds__(32 * (kW + 1), (batch_ring_min_blocks<ST, kW>(
   for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_tile0[k] = a.inst[k].tile0;
   __syncthreads();
   Pol pol{a, s_tile0};
-  tile_pipeline<kW, kStages, Pol::kStageBytes>(smem, pol, tiles, err);
+  tile_pipeline<kW, kStages, Pol::kStageBytes, FlatShape<ST, kW, kC>::kProd>(smem, pol, tiles, err);
 }
 
 template <class ST>

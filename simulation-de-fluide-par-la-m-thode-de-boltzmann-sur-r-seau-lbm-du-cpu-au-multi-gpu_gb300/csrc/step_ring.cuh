@@ -383,16 +383,21 @@ template <class P>
 struct warp_issue<P, std::void_t<decltype(P::kWarpIssue)>> : std::bool_constant<P::kWarpIssue> {};
 
 // Warp-specialised pipeline over tiles 0 .. tiles - 1 (grid-stride) with a ring of kStages
-// stages of kStageBytes: warp 0 (one lane, or all lanes for kWarpIssue policies) calls
-// pol.issue(tile, stage, full_barrier), which arms the barrier with its byte count and issues
-// the bulk copies; consumer warps 1 .. kW wait
+// stages of kStageBytes: the block's j-th tile goes to stage j % kStages (use j / kStages of it)
+// and is issued by producer warp j % kProd (one lane, or all lanes for kWarpIssue policies),
+// which calls pol.issue(tile, stage, full_barrier) to arm the barrier with its byte count and
+// issue the bulk copies. Several producers overlap the issue of consecutive tiles when a
+// policy's issue is long (many short copies per tile); each issues its tiles in increasing j
+// and waits only for the release of tile j - kStages, issued before, so they never wait on one
+// another. Consumer warps kProd .. kProd + kW - 1 wait
 // for the stage, call pol.consume(tile, stage, consumer_warp, lane) and release it. Waits are
-// bounded (error flag). Afterwards every consumer warp (not the producer) calls
+// bounded (error flag). Afterwards every consumer warp (not the producers) calls
 // pol.finish(cw, lane), also after a wait ran out (the host then reports the timeout), e.g. to
 // write the warp's partial sums. Warps never synchronise with one another after the start, so
 // a wait that ran out in one warp cannot leave another waiting at a barrier.
-template <int kW, int kStages, int kStageBytes, class Pol>
+template <int kW, int kStages, int kStageBytes, int kProd = 1, class Pol>
 __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int tiles, int* err) {
+  static_assert(kProd >= 1 && kStages >= 1, "at least one producer warp and one stage");
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * kStageBytes);
   uint64_t* empty = full + kStages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -405,17 +410,20 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
   }
   __syncthreads();
 
-  if (warp == 0) {
+  if (warp < kProd) {
     constexpr bool kWarp = warp_issue<Pol>::value;
     if (!kWarp && lane != 0) return;
-    // Producer.
-    int s = 0, issued = 0;
-    uint32_t phase = 0;
+    // Producer `warp`.
     bool ok = true;
-    for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++issued) {
-      if (issued >= kStages) {
-        const bool got = kWarp ? mbar_wait_bounded_warp(&empty[s], phase ^ 1u, err)
-                               : mbar_wait_bounded(&empty[s], phase ^ 1u, err);
+    int last = -1;
+    for (int j = warp;; j += kProd) {
+      const int tile = blockIdx.x + j * gridDim.x;
+      if (tile >= tiles) break;
+      const int s = j % kStages;
+      if (j >= kStages) {
+        const uint32_t parity = static_cast<uint32_t>((j / kStages - 1) & 1);
+        const bool got = kWarp ? mbar_wait_bounded_warp(&empty[s], parity, err)
+                               : mbar_wait_bounded(&empty[s], parity, err);
         if (!got) {
           ok = false;
           break;
@@ -425,23 +433,18 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
         pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s], lane);
       else
         pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s]);
-      if (++s == kStages) {
-        s = 0;
-        phase ^= 1u;
-      }
+      last = j;
     }
     if (!ok && lane == 0) {
-      for (int k = 0; k < kStages && k < issued; ++k) {
-        const int st = (s + kStages - 1 - k) % kStages;
-        const int use = (issued - 1 - k) / kStages;
-        mbar_wait_bounded(&full[st], static_cast<uint32_t>(use & 1), err);
-      }
+      // Let this producer's copies still in flight land before the block exits.
+      for (int j = last; j >= 0 && j > last - kStages; j -= kProd)
+        mbar_wait_bounded(&full[j % kStages], static_cast<uint32_t>((j / kStages) & 1), err);
     }
     return;
   }
 
   // Consumers.
-  const int cw = warp - 1;
+  const int cw = warp - kProd;
   int s = 0;
   uint32_t phase = 0;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
