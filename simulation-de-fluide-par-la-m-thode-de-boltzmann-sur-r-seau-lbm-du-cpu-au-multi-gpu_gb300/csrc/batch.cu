@@ -124,11 +124,14 @@ __global__ void __launch_bounds__(kBatchThreads)
 
 // Ring tiles of the ensemble. An instance's rows are cut into strips of SW = 32 kC LC cells (one
 // consumer warp's share of a tile, LC = 2 for the 16-bit pairs); its strips are numbered row by
-// row, and a tile is kW consecutive strips of one instance. A tile therefore covers several
-// whole rows of a narrow instance or straddles two rows of a wide one, and every consumer warp
-// has a strip unless the instance's last tile is short: on the benchmark ensemble (row widths
-// 65..1020) 94 % of the lanes of the FP32 8 x 2 shape hold a cell, against 69 % for tiles of one
-// row segment each.
+// row. An instance whose rows fit in a tile (at most kW strips per row) is cut into tiles of
+// whole rows (kW / spr rows each): 9 plane copies (a second one where the rows wrap past the
+// last row) and one per mask row, whatever the row count, at the price of idle lanes and warps.
+// A wider instance is cut into tiles of kW consecutive strips, which straddle two rows (18 copies
+// per row segment). The producer's copy issue is what limits the ensemble, so fewer copies beat
+// fuller lanes: whole-row tiles for every row that fits raised the 256-channel benchmark
+// ensemble (row widths 65..1020) from 99.8k to 106.3k MLUPS with 16-bit storage (8 x 2 shape),
+// against whole-row tiles only for rows of at most half a tile.
 //
 // Stage layout: the tile's rows are segments g = 0 .. nseg - 1 (nseg <= kW). Plane i holds, for
 // each segment, its cells plus a 16-byte halo on each side, segments one after the other: the
@@ -551,9 +554,9 @@ int build_table(lbm_batch* b, int G) {
     d.item0 = item;
     d.spr = (in.nx + b->table_sw - 1) / b->table_sw;
     d.spr_div = FastDiv(static_cast<uint32_t>(d.spr));
-    // Whole-row tiles for instances of at most half a tile per row (few copies per tile);
-    // tiles of consecutive strips otherwise (no idle warps).
-    d.rpt = 2 * d.spr <= b->table_kw ? b->table_kw / d.spr : 0;
+    // Whole-row tiles for instances whose rows fit in a tile (few copies per tile); tiles of
+    // consecutive strips otherwise.
+    d.rpt = d.spr <= b->table_kw ? b->table_kw / d.spr : 0;
     d.tile0 = tile;
     d.k = BForm<ST>::consts(in.tau, in.fx, in.fy);
     item += d.cpr * in.ny;
