@@ -303,7 +303,7 @@ def batch_report(pkg, peak, autotune=True):
         try:
             with pkg.Batch(specs, precision=prec) as b:
                 b.init_equilibrium(1.0, 0.0, 0.0)
-                tune = b.autotune() if autotune else "default: ring 8x2 stages=2 (not tuned)"
+                tune = b.autotune() if autotune else "default: ring 4x2 stages=4 (not tuned)"
                 b.run(64)
                 tb = b.timed_run(640)
                 ts = b.run_separate(64)

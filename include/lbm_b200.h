@@ -269,7 +269,8 @@ int lbm_batch_run_separate(lbm_batch* b, int steps, double* seconds);
  * grid_blocks: blocks (0 = all resident blocks). */
 int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, int grid_blocks);
 /* Tile shape of the ring kernel (selects it): consumer warps x passes per tile, one of 8x2
- * (the default), 4x2, 4x1, 2x2, and the ring depth (2 or 4 stages); a tile spans
+ * (the FP64 default), 4x2 (the FP32 / 16-bit default, with 4 stages), 4x1, 2x2, and the ring
+ * depth (2 or 4 stages); a tile spans
  * warps * passes * 32 cells of a row (twice that with 16-bit storage), so narrow instances waste
  * fewer lanes with smaller shapes, and deeper rings keep more bytes in flight per block. */
 int lbm_batch_set_tiles(lbm_batch* b, int consumer_warps, int passes, int stages);

@@ -148,11 +148,12 @@ struct FlatShape {
   static constexpr int kMaskBytes = kW * 3 * MW * 4;
   static constexpr int kWrapBytes = kW * 6 * 16;
   static constexpr int kStageBytes = kPlaneBytes + kMaskBytes + kWrapBytes;
-  // Producer warps of a ring block: two for FP32, whose many short copies per tile make one
-  // producer the limit on uneven ensembles (measured on the 256-channel benchmark ensemble: 59.0k
-  // -> 65.6k MLUPS); one for the 16-bit forms (a tenth warp would cap their registers below what
-  // their collision needs) and for FP64 (FP64-ALU-bound).
-  static constexpr int kProd = sizeof(ST) == 4 ? 2 : 1;
+  // Producer warps of a ring block: two for FP32 and the 16-bit forms, whose many short copies
+  // per tile make one producer the limit on uneven ensembles (measured on the 256-channel
+  // benchmark ensemble: FP32 59.0k -> 65.6k MLUPS at the same launch; FP16 106.5k -> 113.2k
+  // autotuned, at fewer resident blocks so that the collision keeps its registers); one for
+  // FP64 (FP64-ALU-bound).
+  static constexpr int kProd = sizeof(ST) <= 4 ? 2 : 1;
   static constexpr int kThreads = 32 * (kW + kProd);
   static_assert(SW % 32 == 0 && (SROW * static_cast<int>(sizeof(ST))) % 16 == 0 && kStageBytes % 16 == 0,
                 "stage parts must stay 16-byte aligned");
@@ -426,11 +427,16 @@ __host__ __device__ constexpr size_t batch_ring_smem(int stages) {
   return static_cast<size_t>(stages) * Pol::kStageBytes + 2 * stages * sizeof(uint64_t);
 }
 
-// Resident blocks per SM the register budget of a ring shape is capped for: 27 to 30 warps per SM
-// for the FP32 and 16-bit collisions (72 to 80 registers), none for FP64 (FP64-ALU-bound).
+// Resident blocks per SM the register budget of a ring shape is capped for (blocks of kW
+// consumer and two producer warps): 30 to 32 warps per SM at 64 registers for the FP32
+// collision, 20 to 28 warps at 73 to 80 registers for the 16-bit one (which spills under 72),
+// none for FP64 (FP64-ALU-bound). The autotuner tries no more blocks per SM than this.
+__host__ __device__ constexpr int batch_ring_blocks(int elem, int kW) {
+  return elem == 8 ? 1 : elem == 2 ? (kW == 8 ? 2 : (kW == 4 ? 4 : 7)) : (kW == 8 ? 3 : (kW == 4 ? 5 : 8));
+}
 template <class ST, int kW>
 constexpr int batch_ring_min_blocks() {
-  return sizeof(ST) == 8 ? 1 : (kW == 8 ? 3 : (kW == 4 ? 5 : 8));
+  return batch_ring_blocks(static_cast<int>(sizeof(ST)), kW);
 }
 
 template <class ST, class Phys, int kW, int kC, int kStages>
@@ -939,6 +945,10 @@ int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* con
   b->precision = precision;
   b->elem = elem;
   b->vec = 16 / elem;
+  if (elem != 8) {  // the untuned ring: 4 x 2 tiles, 4 stages (the benchmark ensemble's tuned choice)
+    b->ring_w = 4;
+    b->ring_s = 4;
+  }
   b->host_elem = precision == LBM_FP64 ? 8 : 4;
   b->count = count;
   b->inst.resize(count);
@@ -1164,8 +1174,8 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
   // shared-memory budgets let reside).
   const int shapes[6][3] = {{8, 2, 2}, {4, 2, 2}, {4, 2, 4}, {4, 1, 4}, {2, 2, 2}, {2, 2, 4}};
   for (const auto& sh : shapes)
-    for (int per_sm : {1, 2, 3, 4, 5, 6, 8})
-      if (per_sm <= (sh[0] == 8 ? 3 : (sh[0] == 4 ? 5 : 8))) cands.push_back({1, kBatchThreads, per_sm, sh[0], sh[1], sh[2], 0.0});
+    for (int per_sm : {1, 2, 3, 4, 5, 6, 7, 8})
+      if (per_sm <= batch_ring_blocks(b->elem, sh[0])) cands.push_back({1, kBatchThreads, per_sm, sh[0], sh[1], sh[2], 0.0});
   for (int G : {V, H}) {  // chunk kernel: cells per thread x block x blocks per SM
     if (G == H && H == V) continue;
     for (int blk : {128, 256})
