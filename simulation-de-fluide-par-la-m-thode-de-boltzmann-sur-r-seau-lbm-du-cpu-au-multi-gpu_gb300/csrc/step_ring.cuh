@@ -413,7 +413,41 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
   if (warp < kProd) {
     constexpr bool kWarp = warp_issue<Pol>::value;
     if (!kWarp && lane != 0) return;
-    // Producer `warp`.
+    if constexpr (kProd == 1) {
+      // The single producer: stage and phase advanced incrementally (this form of the loop is
+      // what the producer-bound adjoint kernels were tuned with; the general form below made
+      // them 4-7 % slower).
+      int s = 0, issued = 0;
+      uint32_t phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++issued) {
+        if (issued >= kStages) {
+          const bool got = kWarp ? mbar_wait_bounded_warp(&empty[s], phase ^ 1u, err)
+                                 : mbar_wait_bounded(&empty[s], phase ^ 1u, err);
+          if (!got) {
+            ok = false;
+            break;
+          }
+        }
+        if constexpr (kWarp)
+          pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s], lane);
+        else
+          pol.issue(tile, smem + static_cast<size_t>(s) * kStageBytes, &full[s]);
+        if (++s == kStages) {
+          s = 0;
+          phase ^= 1u;
+        }
+      }
+      if (!ok && lane == 0) {
+        for (int k = 0; k < kStages && k < issued; ++k) {
+          const int st = (s + kStages - 1 - k) % kStages;
+          const int use = (issued - 1 - k) / kStages;
+          mbar_wait_bounded(&full[st], static_cast<uint32_t>(use & 1), err);
+        }
+      }
+      return;
+    }
+    // Producer `warp` of several.
     bool ok = true;
     int last = -1;
     for (int j = warp;; j += kProd) {
