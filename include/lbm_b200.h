@@ -275,8 +275,9 @@ int lbm_batch_set_launch(lbm_batch* b, int cells_per_thread, int block_threads, 
  * fewer lanes with smaller shapes, and deeper rings keep more bytes in flight per block. */
 int lbm_batch_set_tiles(lbm_batch* b, int consumer_warps, int passes, int stages);
 /* Times the candidate launch shapes on the current ensemble and keeps the fastest; with a cache
- * path the choice is read from / appended to that file (one line per GPU, form and size). The
- * state is restored afterwards. report (may be null) receives a one-line summary. */
+ * path the choice is read from / appended to that file (one line per GPU, form, size and kernel
+ * revision). The state is restored afterwards. report (may be null) receives a one-line
+ * summary. */
 int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_t report_size);
 int lbm_batch_info(const lbm_batch* b, int* count, long long* total_cells, int* items);
 

@@ -916,11 +916,16 @@ int time_steps(lbm_batch* b, int steps, double* seconds) {
   return check_batch_flag(b);
 }
 
+// Revision of the batch kernels in autotuner cache keys: raised whenever a change can reorder
+// the candidates or change what a cached launch means (2: two producer warps per ring block and
+// the resident-block caps that come with them), so that older cached choices are timed again.
+constexpr int kBatchKernelRev = 2;
+
 std::string tune_key(const lbm_batch* b) {
   cudaDeviceProp prop{};
   cudaGetDeviceProperties(&prop, b->device);
   std::ostringstream k;
-  k << prop.name << "|p" << b->precision << "|n" << b->count << "|c" << b->total_cells;
+  k << prop.name << "|p" << b->precision << "|n" << b->count << "|c" << b->total_cells << "|r" << kBatchKernelRev;
   return k.str();
 }
 
