@@ -388,8 +388,12 @@ struct warp_issue<P, std::void_t<decltype(P::kWarpIssue)>> : std::bool_constant<
 // which calls pol.issue(tile, stage, full_barrier) to arm the barrier with its byte count and
 // issue the bulk copies. Several producers overlap the issue of consecutive tiles when a
 // policy's issue is long (many short copies per tile); each issues its tiles in increasing j
-// and waits only for the release of tile j - kStages, issued before, so they never wait on one
-// another. Consumer warps kProd .. kProd + kW - 1 wait
+// and waits for the release of tile j - kStages. That parity wait is exact only while the
+// stage's `empty` barrier is at most one phase behind, i.e. tile j - 2 kStages already
+// released: the producer's previous wait (for tile j - kProd - kStages) and the consumers'
+// in-order releases guarantee it when kProd <= kStages, which is therefore required (a model
+// of the schedule under random interleavings: tests/test_pipeline_schedule.py).
+// Consumer warps kProd .. kProd + kW - 1 wait
 // for the stage, call pol.consume(tile, stage, consumer_warp, lane) and release it. Waits are
 // bounded (error flag). Afterwards every consumer warp (not the producers) calls
 // pol.finish(cw, lane), also after a wait ran out (the host then reports the timeout), e.g. to
@@ -398,6 +402,7 @@ struct warp_issue<P, std::void_t<decltype(P::kWarpIssue)>> : std::bool_constant<
 template <int kW, int kStages, int kStageBytes, int kProd = 1, class Pol>
 __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int tiles, int* err) {
   static_assert(kProd >= 1 && kStages >= 1, "at least one producer warp and one stage");
+  static_assert(kProd <= kStages, "a stage's barrier may run two phases behind a producer otherwise");
   uint64_t* full = reinterpret_cast<uint64_t*>(smem + static_cast<size_t>(kStages) * kStageBytes);
   uint64_t* empty = full + kStages;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
