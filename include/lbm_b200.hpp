@@ -42,7 +42,7 @@ namespace lbm {
 
 class SolverB200 {
  public:
-  // Storage form of this build: the reference's `real` selects FP32 or FP64 (both bit-exact
+  // Storage form as compiled: the reference's `real` selects FP32 or FP64 (both bit-exact
   // with v0).
   static constexpr int kPrecision = sizeof(real) == sizeof(double) ? LBM_FP64 : LBM_FP32;
 

@@ -65,7 +65,7 @@ void finish(const Solver& solver, std::size_t n, real* s, real* rho, real* ux, r
 
 extern "C" {
 
-// Size of the reference's `real` in this build (4 or 8).
+// Size of the reference's `real` as compiled (4 or 8).
 int ref_real_size() { return static_cast<int>(sizeof(real)); }
 
 // The reference's mask builders (src/common/geometry.cpp:5-23), row-major nx*ny bytes.
