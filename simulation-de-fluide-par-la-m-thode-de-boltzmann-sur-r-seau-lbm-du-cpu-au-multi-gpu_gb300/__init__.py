@@ -463,9 +463,9 @@ class Batch:
     def set_launch(self, cells_per_thread=0, block_threads=256, grid_blocks=0):
         self._check(lib().lbm_batch_set_launch(self._h, cells_per_thread, block_threads, grid_blocks))
 
-    def set_tiles(self, consumer_warps=8, passes=2, stages=2):
+    def set_tiles(self, consumer_warps=4, passes=2, stages=4):
         """Ring-kernel tile shape (and selects the ring kernel): 8x2, 4x2, 4x1 or 2x2 with 2 or
-        4 ring stages."""
+        4 ring stages. Without a call the library uses 4x2 with 4 stages (8x2 with 2 for FP64)."""
         self._check(lib().lbm_batch_set_tiles(self._h, consumer_warps, passes, stages))
 
     def autotune(self, cache_path=None) -> str:
