@@ -430,7 +430,8 @@ __host__ __device__ constexpr size_t batch_ring_smem(int stages) {
 // Resident blocks per SM the register budget of a ring shape is capped for (blocks of kW
 // consumer and two producer warps): 30 to 32 warps per SM at 64 registers for the FP32
 // collision, 20 to 28 warps at 73 to 80 registers for the 16-bit one (which spills under 72),
-// none for FP64 (FP64-ALU-bound). The autotuner tries no more blocks per SM than this.
+// none for FP64 (FP64-ALU-bound). The autotuner tries no more blocks per SM than this (FP64:
+// up to 3 / 5 / 8 for 8 / 4 / 2 consumer warps, what its registers let reside).
 __host__ __device__ constexpr int batch_ring_blocks(int elem, int kW) {
   return elem == 8 ? 1 : elem == 2 ? (kW == 8 ? 2 : (kW == 4 ? 4 : 7)) : (kW == 8 ? 3 : (kW == 4 ? 5 : 8));
 }
@@ -1180,7 +1181,8 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
   const int shapes[6][3] = {{8, 2, 2}, {4, 2, 2}, {4, 2, 4}, {4, 1, 4}, {2, 2, 2}, {2, 2, 4}};
   for (const auto& sh : shapes)
     for (int per_sm : {1, 2, 3, 4, 5, 6, 7, 8})
-      if (per_sm <= batch_ring_blocks(b->elem, sh[0])) cands.push_back({1, kBatchThreads, per_sm, sh[0], sh[1], sh[2], 0.0});
+      if (per_sm <= (b->elem == 8 ? (sh[0] == 8 ? 3 : (sh[0] == 4 ? 5 : 8)) : batch_ring_blocks(b->elem, sh[0])))
+        cands.push_back({1, kBatchThreads, per_sm, sh[0], sh[1], sh[2], 0.0});
   for (int G : {V, H}) {  // chunk kernel: cells per thread x block x blocks per SM
     if (G == H && H == V) continue;
     for (int blk : {128, 256})
