@@ -193,6 +193,16 @@ int lbm_set_variant(lbm_solver* s, int variant);
  * pitch in elements, and the current read buffer. */
 int lbm_state_view(lbm_solver* s, void** current, long long* plane_stride, int* row_pitch);
 
+/* Test setting, no counterpart in the reference: the limit, in non-blocking polls, of a ring
+ * step kernel's first wait for a staged tile (variants 12-22 of lbm_step / lbm_run, on the
+ * current device, for every solver). 0 restores the default (the ordinary bounded wait). A
+ * small limit makes that wait run out on purpose, so that the failure path can be tested
+ * without a wait that never ends: the kernel sets its error flag, lets every copy it issued
+ * land and finishes without computing the rest of its tiles, and the next synchronising call
+ * (lbm_run, lbm_synchronize, ...) returns LBM_ERR_TIMEOUT and clears the flag. The state is
+ * then invalid until it is set again. */
+int lbm_test_set_consumer_wait_limit(unsigned polls);
+
 /* ---------------------------------------------------------------------------------------------
  * Adjoint (no counterpart in the reference): gradients of a flow objective with respect to the
  * body force, tau and a per-cell Brinkman drag field alpha, as a forward/backward pair.
@@ -328,10 +338,12 @@ int lbm_strips_timed_run(lbm_strips* h, int steps, double* seconds);
  *   stream        cudaStream_t the two kernels are enqueued on (asynchronous; 0 = legacy);
  *   err, err_size optional buffer for a message (may be null).
  * Returns LBM_ERR_INVALID_ARG for null pointers, bad sizes, or ny > LBM_NOALLOC_MAX_ROWS;
- * LBM_ERR_UNSUPPORTED for the 16-bit forms. The first call on a device looks up the device
- * address of the scratch (cudaGetSymbolAddress), so make that first call before any stream
- * capture. All calls share the same scratch and every call rewrites the rows it reads: calls
- * that overlap on the GPU (e.g. on two streams) race and must be serialised by the caller. */
+ * LBM_ERR_UNSUPPORTED for the 16-bit forms. The first call in each CUDA context (the first call
+ * on a device, and again after cudaDeviceReset or in a context the caller creates and makes
+ * current) looks up the device address of the scratch in that context (cudaGetSymbolAddress)
+ * and caches it under the context's id, so make that first call before any stream capture.
+ * All calls share the same scratch and every call rewrites the rows it reads: calls that
+ * overlap on the GPU (e.g. on two streams) race and must be serialised by the caller. */
 int lbm_total_mass_noalloc(const void* planes, int precision, int nx, int ny, int row_pitch,
                            long long plane_stride, const uint8_t* solid, double* mass,
                            void* stream, char* err, size_t err_size);

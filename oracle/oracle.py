@@ -21,13 +21,33 @@ import numpy as np
 HERE = Path(__file__).resolve().parent
 LIB = HERE / "_build" / "liboracle.so"
 REF_DIR = HERE / "_ref"
+# The reference tree: $LBM_REFERENCE_DIR, default /root/reference. Where it is absent (a
+# machine that received only this repository), oracle/Makefile builds from the copy that
+# `make stage` left in oracle/_ref/tree.
+REFERENCE_DIR = Path(os.environ.get("LBM_REFERENCE_DIR", "/root/reference"))
+STAGED_TREE = REF_DIR / "tree"
 
 _u8p = np.ctypeslib.ndpointer(np.uint8, flags="C_CONTIGUOUS")
 
 
-def build(ref: bool = False) -> None:
-    """Compiles the oracle with gcc (flags as oracle/Makefile) and, with ref=True, the reference
-    tree into oracle/_ref (needs make and the reference sources)."""
+def reference_tree() -> Path | None:
+    """The reference tree the Makefile reads (the original, else the staged copy), or None."""
+    for t in (REFERENCE_DIR, STAGED_TREE):
+        if (t / "src" / "v0_cpu" / "solver_v0.cpp").exists():
+            return t
+    return None
+
+
+def _make(*targets: str, env: dict | None = None) -> None:
+    subprocess.run(["make", "-s", "-C", str(HERE), f"-j{os.cpu_count() or 4}", *targets],
+                   check=True, env=env)
+
+
+def build(ref: bool = False, gpu: bool = False) -> None:
+    """Compiles the oracle with gcc (flags as oracle/Makefile); with ref=True, also the
+    reference's own CPU solvers into oracle/_ref (from the reference tree, staging a copy of
+    its files into oracle/_ref/tree when the original is present), and with gpu=True the
+    reference's own GPU solver v3 (needs nvcc)."""
     LIB.parent.mkdir(exist_ok=True)
     src = HERE / "lbm_oracle.c"
     stale = not LIB.exists() or any(p.stat().st_mtime > LIB.stat().st_mtime
@@ -38,9 +58,17 @@ def build(ref: bool = False) -> None:
                         "-fno-trapping-math", "-fopenmp", "-fPIC", "-shared", "-o", str(tmp),
                         str(src)], check=True)
         os.replace(tmp, LIB)
-    if ref:
-        subprocess.run(["make", "-s", "-C", str(HERE), f"-j{os.cpu_count() or 4}", "ref"],
-                       check=True)
+    if ref and reference_tree() is not None:
+        targets = ["ref"] + (["ref-gpu"] if gpu else [])
+        if (REFERENCE_DIR / "src").exists():
+            targets.insert(0, "stage")
+        _make(*targets)
+
+
+def build_consumers(lib_dir: Path) -> None:
+    """Builds the reference's own v3 test programs against the library in lib_dir
+    (oracle/Makefile `consumers`)."""
+    _make("consumers", env={**os.environ, "LBM_LIB": str(lib_dir)})
 
 
 def _dtype(real: str):
@@ -255,9 +283,30 @@ class Reference:
         self.lib.ref_v1_run.restype = C.c_int
         assert self.lib.ref_real_size() == np.dtype(self.dt).itemsize
 
+        for name in ("ref_v0_bench", "ref_v1_bench"):
+            fn = getattr(self.lib, name)
+            fn.restype = C.c_int
+            fn.argtypes = [C.c_int, C.c_int, _u8p, t, t, t, p, C.c_int, C.c_int, C.c_int] + (
+                [C.c_int] if name == "ref_v1_bench" else []) + [dp]
+
     @staticmethod
     def available(real="f32") -> bool:
         return (REF_DIR / f"libref_{real}.so").exists()
+
+    def bench(self, version, nx, ny, solid, tau, fx, fy, s0, steps, *, warmup=1, reps=1,
+              threads=0):
+        """Seconds of each of `reps` timed runs of `steps` steps of v0 or v1 (threads: OpenMP
+        threads of v1, 0 = all) from the post-streaming state s0, after `warmup` steps."""
+        sec = (C.c_double * reps)()
+        s = np.ascontiguousarray(s0, self.dt).reshape(-1)
+        args = [nx, ny, _mask(solid), tau, fx, fy, s, warmup, steps, reps]
+        if version == "v0":
+            rc = self.lib.ref_v0_bench(*args, sec)
+        else:
+            rc = self.lib.ref_v1_bench(*args, threads, sec)
+        if rc != 0:
+            raise ValueError("the reference solver rejected its arguments")
+        return list(sec)
 
     def run(self, version, nx, ny, solid, tau, fx, fy, steps, *, s0=None, init=(1.0, 0.0, 0.0),
             open_x=False, u_in=0.0, threads=0):
@@ -275,3 +324,63 @@ class Reference:
         if rc != 0:
             raise ValueError("the reference solver rejected its arguments")
         return {"s": s, "rho": rho, "ux": ux, "uy": uy, "mass": mass.value}
+
+
+class ReferenceV3:
+    """The reference's own GPU solver SolverV3 (src/v3_cuda_opt/solver_v3.cu, compiled from the
+    unmodified source for sm_103a with --fmad=false by oracle/Makefile `ref-gpu`), run through
+    oracle/ref_v3_shim.cu. Needs a GPU; aborts the process on a CUDA error, as the reference
+    does."""
+
+    def __init__(self, real="f32"):
+        path = REF_DIR / f"libref_v3_{real}.so"
+        if not path.exists():
+            raise FileNotFoundError(path)
+        self.real = real
+        self.dt = _dtype(real)
+        self.lib = C.CDLL(str(path))
+        t = C.c_float if real == "f32" else C.c_double
+        p = np.ctypeslib.ndpointer(self.dt, flags="C_CONTIGUOUS")
+        dp = C.POINTER(C.c_double)
+        self.lib.ref_v3_run.argtypes = [C.c_int, C.c_int, _u8p, t, t, t, C.c_int, t, C.c_int, t,
+                                        t, t, p, C.c_int, p, p, p, dp, C.c_char_p]
+        self.lib.ref_v3_run.restype = C.c_int
+        self.lib.ref_v3_bench.argtypes = [C.c_int, C.c_int, _u8p, t, t, t, p, C.c_int, C.c_int,
+                                          C.c_int, dp, C.c_void_p, C.c_char_p, C.c_size_t,
+                                          C.c_char_p]
+        self.lib.ref_v3_bench.restype = C.c_int
+        assert self.lib.ref_v3_real_size() == np.dtype(self.dt).itemsize
+
+    @staticmethod
+    def available(real="f32") -> bool:
+        return (REF_DIR / f"libref_v3_{real}.so").exists()
+
+    def run(self, nx, ny, solid, tau, fx, fy, steps, *, s0=None, init=(1.0, 0.0, 0.0),
+            open_x=False, u_in=0.0, variant=None):
+        """Same contract as Reference.run; variant: soa_push, soa_pull or soa_pull_opt (the
+        reference's default)."""
+        n = nx * ny
+        s = np.zeros(n * 9, self.dt) if s0 is None else np.array(s0, self.dt, copy=True)
+        rho, ux, uy = (np.empty(n, self.dt) for _ in range(3))
+        mass = C.c_double(0.0)
+        rc = self.lib.ref_v3_run(nx, ny, _mask(solid), tau, fx, fy, int(open_x), u_in,
+                                 int(s0 is None), init[0], init[1], init[2], s, steps, rho, ux,
+                                 uy, C.byref(mass), None if variant is None else variant.encode())
+        if rc != 0:
+            raise ValueError("the reference solver rejected its arguments")
+        return {"s": s, "rho": rho, "ux": ux, "uy": uy, "mass": mass.value}
+
+    def bench(self, nx, ny, solid, tau, fx, fy, s0, steps, *, warmup=10, reps=1,
+              state_out=False, variant=None):
+        """(seconds of each timed_run(steps), bench_info, final populations or None) after
+        `warmup` steps from the post-streaming state s0."""
+        sec = (C.c_double * reps)()
+        out = np.empty(nx * ny * 9, self.dt) if state_out else None
+        info = C.create_string_buffer(1024)
+        rc = self.lib.ref_v3_bench(nx, ny, _mask(solid), tau, fx, fy,
+                                   np.ascontiguousarray(s0, self.dt).reshape(-1), warmup, steps,
+                                   reps, sec, None if out is None else out.ctypes.data, info,
+                                   1024, None if variant is None else variant.encode())
+        if rc != 0:
+            raise ValueError("the reference solver rejected its arguments")
+        return list(sec), info.value.decode(), out

@@ -2,8 +2,10 @@
 // UNMODIFIED reference sources (src/v0_cpu/solver_v0.cpp, src/v1_omp/solver_v1.cpp,
 // src/common/geometry.cpp) by oracle/Makefile into oracle/_ref/libref_{f32,f64}.so.
 //
-// TEST INFRASTRUCTURE ONLY: used by tests/golden/make_golden.py (to produce golden vectors from
-// the reference itself) and by the CPU tests that pin the oracle. Never part of the product.
+// TEST AND MEASUREMENT INFRASTRUCTURE ONLY: used by tests/golden/make_golden.py (to produce
+// golden vectors from the reference itself), by the CPU tests that pin the oracle, and by
+// bench.py's CPU baseline (the reference's own solvers timed on the host cores). Never part of
+// the product.
 //
 // The reference API sets a state only through init_equilibrium() (src/v0_cpu/solver_v0.hpp:21,
 // src/v1_omp/solver_v1.hpp:30). Seeded random initial states need direct access to the
@@ -14,6 +16,7 @@
 // generator checks v0 == v1 bit for bit on every case, which also checks that preimage.
 #include <omp.h>
 
+#include <chrono>
 #include <cstddef>
 #include <cstdint>
 #include <cstring>
@@ -123,6 +126,49 @@ int ref_v1_run(int nx, int ny, const uint8_t* solid, real tau, real fx, real fy,
     }
     solver.run(steps);
     finish(solver, n, s, rho, ux, uy, mass);
+    return 0;
+  } catch (const std::exception&) {
+    return 1;
+  }
+}
+
+// Times a reference CPU solver on an injected state: `warmup` steps, then `reps` repetitions of
+// Solver::run(steps), each timed with std::chrono::steady_clock; seconds[k] receives the k-th.
+// v1 uses `threads` OpenMP threads (0: the OpenMP default). Returns 0, or 1 if the reference
+// threw.
+int ref_v0_bench(int nx, int ny, const uint8_t* solid, real tau, real fx, real fy, const real* s,
+                 int warmup, int steps, int reps, double* seconds) {
+  try {
+    const std::size_t n = static_cast<std::size_t>(nx) * ny;
+    lbm::SolverV0 solver(nx, ny, tau, fx, fy, lbm::Mask(solid, solid + n));
+    solver.g_.assign(s, s + n * 9);
+    solver.g_new_ = solver.g_;
+    solver.run(warmup);
+    for (int k = 0; k < reps; ++k) {
+      const auto t0 = std::chrono::steady_clock::now();
+      solver.run(steps);
+      seconds[k] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
+    return 0;
+  } catch (const std::exception&) {
+    return 1;
+  }
+}
+
+int ref_v1_bench(int nx, int ny, const uint8_t* solid, real tau, real fx, real fy, const real* s,
+                 int warmup, int steps, int reps, int threads, double* seconds) {
+  try {
+    if (threads > 0) omp_set_num_threads(threads);
+    const std::size_t n = static_cast<std::size_t>(nx) * ny;
+    lbm::SolverV1 solver(nx, ny, tau, fx, fy, lbm::Mask(solid, solid + n));
+    s_to_r(nx, ny, solid, 0, s, solver.g_.get());
+    std::memcpy(solver.g_new_.get(), solver.g_.get(), n * 9 * sizeof(real));
+    solver.run(warmup);
+    for (int k = 0; k < reps; ++k) {
+      const auto t0 = std::chrono::steady_clock::now();
+      solver.run(steps);
+      seconds[k] = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    }
     return 0;
   } catch (const std::exception&) {
     return 1;

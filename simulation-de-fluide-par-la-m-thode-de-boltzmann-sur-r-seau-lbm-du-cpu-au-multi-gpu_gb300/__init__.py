@@ -83,6 +83,7 @@ def lib() -> C.CDLL:
             "lbm_strips_timed_run": ([vp, i, C.POINTER(d)], i),
             "lbm_body_force": ([vp, C.POINTER(d), C.POINTER(d)], i),
             "lbm_state_view": ([vp, C.POINTER(vp), C.POINTER(C.c_longlong), C.POINTER(i)], i),
+            "lbm_test_set_consumer_wait_limit": ([C.c_uint], i),
             "lbm_adj_create": ([i, i, vp, d, d, d, i, i, i, C.POINTER(vp)], i),
             "lbm_adj_destroy": ([vp], i),
             "lbm_adj_last_error": ([vp], C.c_char_p),
@@ -463,10 +464,14 @@ class Batch:
     def set_launch(self, cells_per_thread=0, block_threads=256, grid_blocks=0):
         self._check(lib().lbm_batch_set_launch(self._h, cells_per_thread, block_threads, grid_blocks))
 
-    def set_tiles(self, consumer_warps=4, passes=2, stages=4):
+    def set_tiles(self, consumer_warps=None, passes=None, stages=None):
         """Ring-kernel tile shape (and selects the ring kernel): 8x2, 4x2, 4x1 or 2x2 with 2 or
-        4 ring stages. Without a call the library uses 4x2 with 4 stages (8x2 with 2 for FP64)."""
-        self._check(lib().lbm_batch_set_tiles(self._h, consumer_warps, passes, stages))
+        4 ring stages. Arguments left out take the library's default for this precision, the
+        shape used without a call: 4x2 with 4 stages, and 8x2 with 2 stages for FP64."""
+        w, c, s = (8, 2, 2) if self.precision == PRECISIONS["fp64"] else (4, 2, 4)
+        self._check(lib().lbm_batch_set_tiles(
+            self._h, w if consumer_warps is None else consumer_warps,
+            c if passes is None else passes, s if stages is None else stages))
 
     def autotune(self, cache_path=None) -> str:
         buf = C.create_string_buffer(4096)

@@ -430,10 +430,16 @@ __host__ __device__ constexpr size_t batch_ring_smem(int stages) {
 // Resident blocks per SM the register budget of a ring shape is capped for (blocks of kW
 // consumer and two producer warps): 30 to 32 warps per SM at 64 registers for the FP32
 // collision, 20 to 28 warps at 73 to 80 registers for the 16-bit one (which spills under 72),
-// none for FP64 (FP64-ALU-bound). The autotuner tries no more blocks per SM than this (FP64:
-// up to 3 / 5 / 8 for 8 / 4 / 2 consumer warps, what its registers let reside).
+// none for FP64 (FP64-ALU-bound: its kernels are compiled without a register cap).
 __host__ __device__ constexpr int batch_ring_blocks(int elem, int kW) {
   return elem == 8 ? 1 : elem == 2 ? (kW == 8 ? 2 : (kW == 4 ? 4 : 7)) : (kW == 8 ? 3 : (kW == 4 ? 5 : 8));
+}
+// Most resident blocks per SM the autotuner tries for a ring shape: the register cap above,
+// and for FP64 what its uncapped registers let reside (blocks of kW consumer warps and one
+// producer, 82 to 90 registers: 2 / 4 / 6 blocks of 8 / 4 / 2 consumer warps; checked against
+// ptxas by tests/test_register_budget.py).
+__host__ __device__ constexpr int batch_ring_tune_blocks(int elem, int kW) {
+  return elem == 8 ? (kW == 8 ? 2 : (kW == 4 ? 4 : 6)) : batch_ring_blocks(elem, kW);
 }
 template <class ST, int kW>
 constexpr int batch_ring_min_blocks() {
@@ -1168,12 +1174,40 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
     }
   }
   // Time every candidate on the current state; the state and the step counter advance, which
-  // is harmless for timing, and both are put back from a saved copy afterwards.
+  // is harmless for timing, and both are put back from a saved copy afterwards, on success and
+  // on every error exit, together with the launch shape the ensemble had on entry.
   const uint32_t t_saved = b->t;
+  const int entry_G = b->G, entry_block = b->block, entry_grid = b->grid;
+  const int entry_w = b->ring_w, entry_c = b->ring_c, entry_s = b->ring_s;
   const size_t bytes = static_cast<size_t>(b->total_elems) * b->elem + 256;
   void* saved = nullptr;
   B_CUDA(b, cudaMalloc(&saved, bytes));
   B_CUDA(b, cudaMemcpyAsync(saved, b->buf[b->cur], bytes, cudaMemcpyDeviceToDevice, b->stream));
+  auto restore = [&](bool entry_shape) {
+    const cudaError_t e1 =
+        cudaMemcpyAsync(b->buf[b->cur], saved, bytes, cudaMemcpyDeviceToDevice, b->stream);
+    step_counter_set<<<1, 1, 0, b->stream>>>(b->step_d, t_saved);
+    b->t = t_saved;
+    const cudaError_t e2 = cudaStreamSynchronize(b->stream);
+    cudaFree(saved);
+    if (entry_shape) {
+      b->G = entry_G;
+      b->block = entry_block;
+      b->grid = entry_grid;
+      b->ring_w = entry_w;
+      b->ring_c = entry_c;
+      b->ring_s = entry_s;
+      drop_graph(b);
+    }
+    return e1 != cudaSuccess ? e1 : e2;
+  };
+  // An error exit: state, step counter and launch shape back as on entry, the first error kept.
+  auto fail_restored = [&](int rc) {
+    const std::string msg = b->err;
+    restore(true);
+    b->err = msg;
+    return rc;
+  };
   const int V = b->vec, H = V / 2 >= 2 ? V / 2 : V;
   std::vector<Cand> cands;
   // Ring kernel: tile shape x stages x resident blocks per SM (up to what the register and
@@ -1181,7 +1215,7 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
   const int shapes[6][3] = {{8, 2, 2}, {4, 2, 2}, {4, 2, 4}, {4, 1, 4}, {2, 2, 2}, {2, 2, 4}};
   for (const auto& sh : shapes)
     for (int per_sm : {1, 2, 3, 4, 5, 6, 7, 8})
-      if (per_sm <= (b->elem == 8 ? (sh[0] == 8 ? 3 : (sh[0] == 4 ? 5 : 8)) : batch_ring_blocks(b->elem, sh[0])))
+      if (per_sm <= batch_ring_tune_blocks(b->elem, sh[0]))
         cands.push_back({1, kBatchThreads, per_sm, sh[0], sh[1], sh[2], 0.0});
   for (int G : {V, H}) {  // chunk kernel: cells per thread x block x blocks per SM
     if (G == H && H == V) continue;
@@ -1195,19 +1229,10 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
   Cand pick = cands.front();
   std::ostringstream rep;
   for (Cand& c : cands) {
-    if (int rc = apply(c)) {
-      cudaFree(saved);
-      return rc;
-    }
+    if (int rc = apply(c)) return fail_restored(rc);
     double t = 0.0;
-    if (int rc = time_steps(b, 4, &t)) {  // warm-up
-      cudaFree(saved);
-      return rc;
-    }
-    if (int rc = time_steps(b, 16, &t)) {
-      cudaFree(saved);
-      return rc;
-    }
+    if (int rc = time_steps(b, 4, &t)) return fail_restored(rc);  // warm-up
+    if (int rc = time_steps(b, 16, &t)) return fail_restored(rc);
     c.t = t;
     rep << (c.G <= 1 ? "R" + std::to_string(c.w) + "x" + std::to_string(c.c) + "s" + std::to_string(c.s)
                      : "G" + std::to_string(c.G) + "/b" + std::to_string(c.blk))
@@ -1217,11 +1242,7 @@ int lbm_batch_autotune(lbm_batch* b, const char* cache_path, char* report, size_
       pick = c;
     }
   }
-  B_CUDA(b, cudaMemcpyAsync(b->buf[b->cur], saved, bytes, cudaMemcpyDeviceToDevice, b->stream));
-  step_counter_set<<<1, 1, 0, b->stream>>>(b->step_d, t_saved);
-  b->t = t_saved;
-  B_CUDA(b, cudaStreamSynchronize(b->stream));
-  cudaFree(saved);
+  B_CUDA(b, restore(false));
   if (int rc = apply(pick)) return rc;
   b->tune_report = "tuned: " + describe(pick) + " | " + rep.str();
   if (cache_path) {

@@ -12,6 +12,7 @@
 // limit kNoAllocMaxRows. Every call rewrites all the rows it uses before reading them, so nothing
 // needs clearing, but all calls share the same arrays: two calls that overlap on the GPU (for
 // example on two streams) race on them.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <cstdint>
@@ -23,21 +24,37 @@
 namespace {
 
 constexpr int kNoAllocMaxRows = 16384;  // LBM_NOALLOC_MAX_ROWS in the header
-constexpr int kMaxDevices = 64;
 static_assert(kNoAllocMaxRows == LBM_NOALLOC_MAX_ROWS, "header and library disagree");
 
 static __device__ __align__(256) double g_row_sum[kNoAllocMaxRows];
 static __device__ __align__(256) unsigned long long g_row_fluid[kNoAllocMaxRows];
 
-// Device addresses of the scratch arrays, looked up once per device. In host code the names
-// above are host-side stand-ins, not device addresses, so they must never be passed to a kernel.
+// Device addresses of the scratch arrays. In host code the names above are host-side
+// stand-ins, not device addresses, so they must never be passed to a kernel. The addresses
+// belong to the copy of this module loaded in one CUDA context: every device's primary context
+// has its own, a context that the caller creates and makes current (driver API) loads another,
+// and cudaDeviceReset discards them. They are therefore looked up once per context and cached
+// under the context's process-unique id (cuCtxGetId, which is never reused, unlike a context
+// handle), so that a stale address is never handed to a kernel.
 struct ScratchAddr {
+  unsigned long long ctx_id = 0;
   double* row_sum = nullptr;
   unsigned long long* row_fluid = nullptr;
   bool ready = false;
 };
+constexpr int kMaxContexts = 64;
 std::mutex g_mu;
-ScratchAddr g_addr[kMaxDevices];
+ScratchAddr g_addr[kMaxContexts];
+int g_next_slot = 0;
+
+// The two driver calls that identify the current context, reached through the runtime's
+// entry-point query so that the library does not link against libcuda.
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+CtxGetCurrentFn g_ctx_get_current = nullptr;
+CtxGetIdFn g_ctx_get_id = nullptr;
+std::once_flag g_driver_once;
+bool g_driver_ok = false;
 
 // Pass 1: one warp per row. Per fluid cell the 9 stored populations are added in order
 // i = 0..8 in double; lanes take the columns x = lane, lane + 32, ...; the warp then combines
@@ -116,24 +133,47 @@ int report(char* err, size_t err_size, int code, const char* msg) {
   return code;
 }
 
-// Looks up the device addresses of the scratch arrays on the current device (first call on
-// each device only).
-int scratch_for_current_device(ScratchAddr* out, char* err, size_t err_size) {
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
+// Process-unique id of the context current on this thread; false if there is none yet or the
+// driver cannot tell.
+bool current_context_id(unsigned long long* id) {
+  std::call_once(g_driver_once, [] {
+    cudaDriverEntryPointQueryResult q1 = cudaDriverEntryPointSymbolNotFound, q2 = q1;
+    const cudaError_t e1 = cudaGetDriverEntryPointByVersion(
+        "cuCtxGetCurrent", reinterpret_cast<void**>(&g_ctx_get_current), 12000,
+        cudaEnableDefault, &q1);
+    const cudaError_t e2 = cudaGetDriverEntryPointByVersion(
+        "cuCtxGetId", reinterpret_cast<void**>(&g_ctx_get_id), 12000, cudaEnableDefault, &q2);
+    g_driver_ok = e1 == cudaSuccess && e2 == cudaSuccess && q1 == cudaDriverEntryPointSuccess &&
+                  q2 == cudaDriverEntryPointSuccess && g_ctx_get_current && g_ctx_get_id;
+  });
+  if (!g_driver_ok) return false;
+  CUcontext ctx = nullptr;
+  if (g_ctx_get_current(&ctx) != CUDA_SUCCESS || ctx == nullptr) return false;
+  return g_ctx_get_id(ctx, id) == CUDA_SUCCESS;
+}
+
+// Device addresses of the scratch arrays in the current context: from the cache, or looked up
+// with cudaGetSymbolAddress (the first call in each context; it also makes the runtime bind
+// its context if none is current yet) and cached under the context's id.
+int scratch_for_current_context(ScratchAddr* out, char* err, size_t err_size) {
+  unsigned long long id = 0;
+  if (current_context_id(&id)) {
+    std::lock_guard<std::mutex> lock(g_mu);
+    for (const ScratchAddr& a : g_addr)
+      if (a.ready && a.ctx_id == id) {
+        *out = a;
+        return LBM_OK;
+      }
+  }
+  ScratchAddr a;
+  cudaError_t e = cudaGetSymbolAddress(reinterpret_cast<void**>(&a.row_sum), g_row_sum);
+  if (e == cudaSuccess) e = cudaGetSymbolAddress(reinterpret_cast<void**>(&a.row_fluid), g_row_fluid);
   if (e != cudaSuccess) return report(err, err_size, LBM_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices)
-    return report(err, err_size, LBM_ERR_UNSUPPORTED, "device index beyond the supported range");
-  std::lock_guard<std::mutex> lock(g_mu);
-  ScratchAddr& a = g_addr[dev];
-  if (!a.ready) {
-    e = cudaGetSymbolAddress(reinterpret_cast<void**>(&a.row_sum), g_row_sum);
-    if (e == cudaSuccess) e = cudaGetSymbolAddress(reinterpret_cast<void**>(&a.row_fluid), g_row_fluid);
-    if (e != cudaSuccess) {
-      a = ScratchAddr{};
-      return report(err, err_size, LBM_ERR_CUDA, cudaGetErrorString(e));
-    }
+  if (current_context_id(&a.ctx_id)) {
     a.ready = true;
+    std::lock_guard<std::mutex> lock(g_mu);
+    g_addr[g_next_slot] = a;  // the oldest entry goes first once the table is full
+    g_next_slot = (g_next_slot + 1) % kMaxContexts;
   }
   *out = a;
   return LBM_OK;
@@ -156,7 +196,7 @@ extern "C" int lbm_total_mass_noalloc(const void* planes, int precision, int nx,
   if (precision != LBM_FP32 && precision != LBM_FP64)
     return report(err, err_size, LBM_ERR_UNSUPPORTED, "only LBM_FP32 and LBM_FP64 states");
   ScratchAddr a;
-  if (int rc = scratch_for_current_device(&a, err, err_size)) return rc;
+  if (int rc = scratch_for_current_context(&a, err, err_size)) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int threads = 256;
   const int blocks = (ny + (threads / 32) - 1) / (threads / 32);

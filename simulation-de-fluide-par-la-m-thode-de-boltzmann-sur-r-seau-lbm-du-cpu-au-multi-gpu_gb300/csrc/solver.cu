@@ -928,7 +928,7 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks) {
 int lbm_set_variant(lbm_solver* s, int variant) {
   if (check(s)) return LBM_ERR_INVALID_ARG;
   if (variant < -1 || variant > 22)
-    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 17]");
+    return set_error(s, LBM_ERR_INVALID_ARG, "variant must be in [-1, 22]");
   s->variant = variant;
   lbm_b200::drop_step_graph(s);
   return LBM_OK;
@@ -940,6 +940,12 @@ int lbm_state_view(lbm_solver* s, void** current, long long* plane_stride, int* 
   if (plane_stride) *plane_stride = s->g.plane;
   if (row_pitch) *row_pitch = s->g.pitch;
   return LBM_OK;
+}
+
+int lbm_test_set_consumer_wait_limit(unsigned polls) {
+  const unsigned v = polls == 0 || polls >= lbm_b200::kSpinLimit ? lbm_b200::kSpinLimit : polls;
+  const cudaError_t e = cudaMemcpyToSymbol(lbm_b200::c_consumer_wait_limit, &v, sizeof v);
+  return e == cudaSuccess ? LBM_OK : LBM_ERR_CUDA;
 }
 
 }  // extern "C"

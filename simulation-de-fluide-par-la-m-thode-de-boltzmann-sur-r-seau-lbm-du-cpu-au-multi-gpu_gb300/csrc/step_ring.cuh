@@ -395,7 +395,8 @@ struct warp_issue<P, std::void_t<decltype(P::kWarpIssue)>> : std::bool_constant<
 // of the schedule under random interleavings: tests/test_pipeline_schedule.py).
 // Consumer warps kProd .. kProd + kW - 1 wait
 // for the stage, call pol.consume(tile, stage, consumer_warp, lane) and release it. Waits are
-// bounded (error flag). Afterwards every consumer warp (not the producers) calls
+// bounded (error flag; a consumer whose first wait ran out under the test limit drains, see
+// consumer_wait_full). Afterwards every consumer warp (not the producers) calls
 // pol.finish(cw, lane), also after a wait ran out (the host then reports the timeout), e.g. to
 // write the warp's partial sums. Warps never synchronise with one another after the start, so
 // a wait that ran out in one warp cannot leave another waiting at a barrier.
@@ -482,13 +483,17 @@ __device__ __forceinline__ void tile_pipeline(unsigned char* smem, Pol& pol, int
     return;
   }
 
-  // Consumers.
+  // Consumers. A warp whose wait ran out under the test limit drains (consumer_wait_full).
   const int cw = warp - kProd;
   int s = 0;
   uint32_t phase = 0;
+  bool drain = false;
   for (int tile = blockIdx.x; tile < tiles; tile += gridDim.x) {
-    if (!mbar_wait_bounded_warp(&full[s], phase, err)) break;
-    pol.consume(tile, smem + static_cast<size_t>(s) * kStageBytes, cw, lane);
+    const int got = drain ? (mbar_wait_bounded_warp(&full[s], phase, err) ? 2 : 0)
+                          : consumer_wait_full(&full[s], phase, err);
+    if (!got) break;
+    drain = got == 2;
+    if (!drain) pol.consume(tile, smem + static_cast<size_t>(s) * kStageBytes, cw, lane);
     __syncwarp();
     if (lane == 0) mbar_arrive(&empty[s]);
     if (++s == kStages) {

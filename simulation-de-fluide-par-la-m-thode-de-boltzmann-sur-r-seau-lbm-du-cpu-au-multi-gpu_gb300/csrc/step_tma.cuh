@@ -94,6 +94,44 @@ __device__ __forceinline__ bool mbar_wait_bounded_warp(uint64_t* bar, uint32_t p
   return false;
 }
 
+// Non-blocking test of a phase's completion (one poll, no suspension).
+__device__ __forceinline__ bool mbar_test_wait(uint64_t* bar, uint32_t parity) {
+  uint32_t done;
+  asm volatile(
+      "{\n"
+      ".reg .pred p;\n"
+      "mbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+      "selp.u32 %0, 1, 0, p;\n"
+      "}\n"
+      : "=r"(done)
+      : "r"(smem_addr(bar)), "r"(parity)
+      : "memory");
+  return done != 0;
+}
+
+// Limit of a ring consumer's first wait for a full stage (tile_pipeline, step_ring.cuh), in
+// non-blocking polls. kSpinLimit, the default, selects the ordinary bounded wait. A smaller
+// value is a test setting (lbm_test_set_consumer_wait_limit, solver.cu) that makes the wait run
+// out on purpose: the consumer warp then sets the error flag and drains, i.e. waits (bounded,
+// blocking) for that stage and every later stage of its block and releases them without
+// computing, so the producer is never left waiting and no copy is still in flight into a block
+// that has exited. Each translation unit holds its own copy; only the solver's is settable.
+static __constant__ unsigned c_consumer_wait_limit = kSpinLimit;
+
+// A consumer warp's wait for a full stage: 1 = data ready, 2 = the test limit ran out (error
+// flag set) and the stage's copies have landed (drain from here on), 0 = a bounded wait ran
+// out (error flag set).
+__device__ __forceinline__ int consumer_wait_full(uint64_t* bar, uint32_t parity, int* err) {
+  const unsigned limit = c_consumer_wait_limit;
+  if (limit < kSpinLimit) {
+    for (unsigned it = 0; it < limit; ++it)
+      if (__all_sync(0xffffffffu, mbar_test_wait(bar, parity))) return 1;
+    if ((threadIdx.x & 31) == 0) atomicExch(err, 1);
+    return mbar_wait_bounded_warp(bar, parity, err) ? 2 : 0;
+  }
+  return mbar_wait_bounded_warp(bar, parity, err) ? 1 : 0;
+}
+
 // One-dimensional bulk copy global -> shared, completing `bytes` on the mbarrier.
 __device__ __forceinline__ void bulk_copy_g2s(void* dst_smem, const void* src_gmem, uint32_t bytes,
                                               uint64_t* bar) {

@@ -69,27 +69,89 @@ WAKE_FORCE = 6.784303312490499e-07
 
 def lift_series(pkg, precision: str, steps: int = 200_000, every: int = 50, variant: int = -1,
                 nx: int = NX, ny: int = NY, d: float = D, tau: float = TAU, u0: float = U0,
-                force: float | None = None):
+                force: float | None = None, mean_every: int = 0):
     """Runs the wake and samples the force on the disc every `every` steps. Returns a dict of
-    numpy arrays t, drag, lift and the bulk velocity u_bulk at the end."""
+    numpy arrays t, drag, lift, the bulk velocity u_bulk, the final velocity field (ux_end,
+    uy_end, float64) and the total mass at the start and the end (mass0, mass1). With
+    mean_every > 0 (a multiple of `every`), also the velocity field averaged over the second
+    half of the run, sampled every mean_every steps (ux_mean, uy_mean)."""
     solid, disc = geometry(nx, ny, d)
     fx = force if force is not None else (WAKE_FORCE or wake_force(tau, u0, ny - 2))
     n = steps // every
     t = np.arange(1, n + 1) * every
     drag, lift = np.empty(n), np.empty(n)
+    acc_x = acc_y = None
+    n_mean = 0
     with pkg.Solver(nx, ny, tau, fx, 0.0, solid, precision=precision) as s:
         if variant >= 0:
             s.set_variant(variant)
         s.init_equilibrium(1.0, u0, 0.0)
         s.set_body(disc)
+        mass0 = s.total_mass()
         for k in range(n):
             s.run(every)
             drag[k], lift[k] = s.body_force()
-        _, ux, _ = s.macroscopic()
+            if mean_every and t[k] > steps // 2 and t[k] % mean_every == 0:
+                _, ux, uy = s.macroscopic()
+                if acc_x is None:
+                    acc_x, acc_y = np.zeros(ux.size), np.zeros(uy.size)
+                acc_x += ux
+                acc_y += uy
+                n_mean += 1
+        _, ux, uy = s.macroscopic()
+        mass1 = s.total_mass()
         finite = s.check_finite()
     fluid = solid == 0
-    return {"t": t, "drag": drag, "lift": lift, "u_bulk": float(np.mean(ux[fluid])),
-            "finite": finite, "d": d}
+    out = {"t": t, "drag": drag, "lift": lift, "u_bulk": float(np.mean(ux[fluid])),
+           "finite": finite, "d": d, "fluid": fluid, "ux_end": ux.astype(np.float64),
+           "uy_end": uy.astype(np.float64), "mass0": mass0, "mass1": mass1}
+    if n_mean:
+        out["ux_mean"], out["uy_mean"] = acc_x / n_mean, acc_y / n_mean
+    return out
+
+
+def velocity_l2(run, ref, which: str = "mean") -> float:
+    """Relative L2 error over fluid cells of a run's velocity field against a reference run's:
+    which = "mean" (the second-half mean flow) or "end" (the final field)."""
+    fluid = ref["fluid"]
+    ux, uy = run[f"ux_{which}"][fluid], run[f"uy_{which}"][fluid]
+    rx, ry = ref[f"ux_{which}"][fluid], ref[f"uy_{which}"][fluid]
+    num = np.sum((ux - rx) ** 2 + (uy - ry) ** 2)
+    den = np.sum(rx * rx + ry * ry)
+    return float(np.sqrt(num / den)) if den > 0 else float("nan")
+
+
+def probe_strouhal(out_dir, start: float = 0.5) -> dict:
+    """Strouhal number of an open-BC cylinder run from the driver's probe.csv and meta.json,
+    measured as the reference's analysis does (scripts/strouhal.py:57-86): after discarding
+    the first `start` fraction of the steps, the shedding frequency of u_y - mean(u_y) at the
+    probe (a) at the peak of its spectrum (Hann window, zero padding to 16x, parabolic
+    interpolation of the log magnitude around the maximum) and (b) from the mean period between
+    upward zero crossings (crossing times by linear interpolation); St = f D / u_in."""
+    from pathlib import Path
+    import json
+
+    out_dir = Path(out_dir)
+    meta = json.loads((out_dir / "meta.json").read_text())
+    data = np.loadtxt(out_dir / "probe.csv", delimiter=",", skiprows=1)
+    step, uy = data[:, 0], data[:, 2]
+    keep = step >= start * meta["steps"]
+    step, uy = step[keep], uy[keep] - uy[keep].mean()
+    dt = float(step[1] - step[0])
+    d, u = meta["diameter"], meta["u_in"]
+    n = len(uy)
+    mag = np.abs(np.fft.rfft(uy * np.hanning(n), 16 * n))
+    freq = np.fft.rfftfreq(16 * n, d=dt)
+    k = int(np.argmax(mag[1:]) + 1)
+    a, b, c = np.log(mag[k - 1:k + 2] + 1e-300)
+    f_fft = (k + 0.5 * (a - c) / (a - 2.0 * b + c)) * (freq[1] - freq[0])
+    up = np.flatnonzero((uy[:-1] < 0) & (uy[1:] >= 0))
+    t_cross = step[up] - uy[up] * (step[up + 1] - step[up]) / (uy[up + 1] - uy[up])
+    periods = np.diff(t_cross)
+    f_zero = 1.0 / periods.mean() if len(periods) else float("nan")
+    return {"st_fft": float(f_fft * d / u), "st_zero_crossing": float(f_zero * d / u),
+            "periods": int(len(periods)), "uy_amplitude": float(np.abs(uy).max()),
+            "window_start": int(start * meta["steps"]), "real": meta["real"]}
 
 
 def strouhal(series, tail: float = 0.5):

@@ -55,6 +55,15 @@ def brinkman_field(nx: int, ny: int, seed: int, n_gauss: int = 16, wmin: float =
     return (alpha_max * g).reshape(-1)
 
 
+def brinkman_batch(nx: int, ny: int, count: int, solid, seed: int) -> np.ndarray:
+    """`count` distinct drag fields (brinkman_field of seeds seed, seed + 1, ...), zero on solid
+    cells: a (count, nx * ny) array, the adjoint workload's batch of alpha fields."""
+    fluid = np.asarray(solid).reshape(-1) == 0
+    out = np.stack([brinkman_field(nx, ny, seed + k) for k in range(count)])
+    out[:, ~fluid] = 0.0
+    return out
+
+
 def adjoint_channel(nx: int = 512, ny: int = 128):
     """The adjoint workload's geometry: walled channel, periodic in x (tau 0.6, F = (5e-6, 0))."""
     return make_channel(nx, ny)

@@ -5,6 +5,7 @@ done by this script). Run from the repository root:
 
     python tests/golden/make_golden.py            # small cases (.npz) and large-case hashes
     python tests/golden/make_golden.py --small    # small cases only
+    python tests/golden/make_golden.py --wake     # cylinder-wake digests only (minutes)
 
 For every case both reference solvers run, v0 (sequential, push) and v1 (OpenMP, pull), and the
 script checks that they agree bit for bit before writing anything. States injected with a seeded
@@ -14,7 +15,9 @@ it as is, v1 receives its preimage by streaming, so the v0 == v1 check also pins
 Small cases are stored whole (inputs and outputs, float and double). The at-scale channel
 cases (2048^2 x 1000 steps, 4096^2, 8192^2) are stored as SHA-256 digests of the outputs, with
 negative zeros mapped to +0 first (the reference's own tests compare with `!=`, which treats
--0 and +0 as equal).
+-0 and +0 as equal). The cylinder-wake workload (walled channel 1024 x 256 with a disc of
+diameter 32 at (256, 129), tau 0.548, calibrated body force, uniform start u = (0.05, 0),
+200k steps) is stored the same way in wake_hashes.json, float and double.
 """
 from __future__ import annotations
 
@@ -235,12 +238,46 @@ def make_large(only=None):
         path.write_text(json.dumps(out, indent=1) + "\n")
 
 
+# The cylinder-wake workload's body force, calibrated once for a bulk velocity of 0.05 (the
+# library's wake.WAKE_FORCE; repeated here so that this script needs only the reference).
+WAKE_FORCE = 6.784303312490499e-07
+
+
+def make_wake(steps=200_000):
+    """Reference v1 digests of the cylinder-wake workload after `steps` steps."""
+    path = OUT / "wake_hashes.json"
+    out = {}
+    threads = os.cpu_count() or 4
+    nx, ny = 1024, 256
+    mask = (ref_channel(nx, ny) | ref_cylinder(nx, ny, 256.0, 129.0, 32.0)).astype(np.uint8)
+    for real in ("f32", "f64"):
+        case = dict(nx=nx, ny=ny, mask=mask, tau=0.548, fx=WAKE_FORCE, fy=0.0, steps=steps,
+                    init=(1.0, 0.05, 0.0))
+        t0 = time.time()
+        r, _ = run_ref(case, real, "v1", threads=threads)
+        dt = time.time() - t0
+        out[f"wake_{real}"] = {
+            "nx": nx, "ny": ny, "real": real, "steps": steps, "tau": 0.548, "fx": WAKE_FORCE,
+            "fy": 0.0, "init": [1.0, 0.05, 0.0], "mask": "channel | cylinder(256, 129, D 32)",
+            "mask_sha": hashlib.sha256(mask.tobytes()).hexdigest(),
+            "s": digest(r["s"]), "rho": digest(r["rho"]), "ux": digest(r["ux"]),
+            "uy": digest(r["uy"]), "mass": r["mass"],
+            "generator": "reference v1 (src/v1_omp/solver_v1.cpp), %d threads" % threads,
+        }
+        print(f"wake_{real}: reference v1 {dt:.1f} s, {nx * ny * steps / dt / 1e6:.0f} MLUPS")
+        path.write_text(json.dumps(out, indent=1) + "\n")
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--small", action="store_true")
     ap.add_argument("--large", nargs="*", default=None)
+    ap.add_argument("--wake", action="store_true")
     args = ap.parse_args()
     oracle.build(ref=True)
+    if args.wake:
+        make_wake()
+        return
     if args.large is None:
         make_small()
     if not args.small:

@@ -122,6 +122,30 @@ def test_batch_of_alpha_fields(setup):
         np.testing.assert_allclose(gb["alpha"][k], g1["alpha"][0], rtol=1e-9, atol=1e-18)
 
 
+def test_batch_of_32_seeded_fields_full_run(setup):
+    """The adjoint benchmark's batch: 32 distinct seeded alpha fields (seeds 1234..1265), the
+    full 2000 steps with checkpoints every 100, FP32; instances 0 and 31 against single runs
+    of their own fields."""
+    pkg, mask, _, _ = setup
+    fields = pkg.workloads.brinkman_batch(NX, NY, 32, mask, seed=1234)
+    assert not np.array_equal(fields[0], fields[1])
+    with pkg.Adjoint(NX, NY, TAU, FX, 0.0, mask, precision="fp32", batch=32, checkpoint_every=K) as a:
+        a.set_alpha(fields)
+        Jb = a.forward(STEPS, WINDOW)
+        gb = a.backward()
+    assert len(set(np.round(Jb, 12))) == 32
+    for k in (0, 31):
+        with pkg.Adjoint(NX, NY, TAU, FX, 0.0, mask, precision="fp32", checkpoint_every=K) as a:
+            a.set_alpha(fields[k])
+            J1 = a.forward(STEPS, WINDOW)[0]
+            g1 = a.backward()
+        assert Jb[k] == pytest.approx(J1, rel=1e-6)
+        assert gb["fx"][k] == pytest.approx(g1["fx"][0], rel=1e-5)
+        assert gb["tau"][k] == pytest.approx(g1["tau"][0], rel=1e-5)
+        scale = np.max(np.abs(g1["alpha"][0]))
+        np.testing.assert_allclose(gb["alpha"][k], g1["alpha"][0], rtol=1e-5, atol=1e-6 * scale)
+
+
 def test_backward_cost_within_3x_forward(setup):
     pkg, mask, alpha, _ = setup
     with pkg.Adjoint(NX, NY, TAU, FX, 0.0, mask, precision="fp32", batch=32, checkpoint_every=K) as a:

@@ -4,7 +4,10 @@ Workload shape: seeded channels nx ~ U[64, 1024], ny ~ U[32, 512], 1-4 discs of 
 clear of the walls, tau ~ U[0.52, 1.0], fx ~ U[1e-6, 1e-5], seeded initial perturbation.
 Checks: 8 sampled instances bit-exact against the oracle's port of the reference v1 solver (itself
 pinned bit for bit to the reference v0); batched == one launch per instance, every launch shape;
-the autotuner leaves the state unchanged; the FP16-storage batch stays close to FP32.
+the autotuner leaves the state unchanged; the FP16-storage batch stays close to FP32. The
+benchmark's own ensemble (256 instances, seed 7, 5000 steps from rest, autotuned launch) is
+checked on 8 seeded sampled instances against the reference's own v1 solver where it was built
+(else the oracle's port).
 """
 from __future__ import annotations
 
@@ -163,3 +166,28 @@ def test_odd_widths_bit_exact(gpu_lib, orc):
             r = orc.s_to_r(nx, ny, m, orc.seeded_state(s["seed"], 1e-4, nx, ny, m))
             orc.pull_run(nx, ny, m, float(np.float32(s["tau"])), s["fx"], 0.0, r, 60)
             assert np.array_equal(b.populations(k), orc.r_to_s(nx, ny, m, r)), f"instance {k} ({nx}x{ny})"
+
+
+def test_benchmark_ensemble_sampled_instances_bit_exact(gpu_lib, orc):
+    """The batched benchmark's workload as timed by bench.py: 256 channels of seed 7, rest
+    start, the autotuned launch, 5000 steps; 8 instances picked by seed."""
+    specs = gpu_lib.workloads.ensemble_specs(256, seed=7)
+    picks = sorted({int(v * 256) for v in gpu_lib.workloads.uniform01(2024, 8)})
+    steps = 5000
+    with gpu_lib.Batch(specs, precision="fp32") as b:
+        b.init_equilibrium(1.0, 0.0, 0.0)
+        b.autotune()
+        b.run(steps)
+        got = {k: b.populations(k) for k in picks}
+    ref = orc.Reference("f32") if orc.Reference.available("f32") else None
+    for k in picks:
+        s = specs[k]
+        nx, ny, m = s["nx"], s["ny"], s["mask"]
+        tau = float(np.float32(s["tau"]))
+        if ref is not None:
+            want = ref.run("v1", nx, ny, m, tau, s["fx"], 0.0, steps, init=(1.0, 0.0, 0.0))["s"]
+        else:
+            r = orc.s_to_r(nx, ny, m, orc.init_equilibrium(nx, ny, m, 1.0, 0.0, 0.0))
+            orc.pull_run(nx, ny, m, tau, s["fx"], 0.0, r, steps)
+            want = orc.r_to_s(nx, ny, m, r)
+        assert np.array_equal(got[k], want), f"instance {k} ({nx}x{ny})"

@@ -5,18 +5,24 @@ instantiates, with lbm::SolverB200 in place of lbm::SolverV3:
   - poiseuille::run_all<Solver>   (reference tests/poiseuille_check.hpp:128-158)
   - cylinder_case::run<Solver>    (reference tests/cylinder_case.hpp:33-41)
   - lbm::run_driver<Solver>       (reference src/common/driver.hpp:255-300)
-in float and double. Needs the reference tree (skipped without it).
+in float and double. Needs the reference tree or its staged copy (skipped without either). The
+GPU test tests/test_reference_gpu.py builds and runs the reference's own v3 test programs
+against the library.
 """
 from __future__ import annotations
 
 import shutil
 import subprocess
+import sys
 from pathlib import Path
 
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path("/root/reference")
+sys.path.insert(0, str(ROOT / "oracle"))
+import oracle  # noqa: E402  (test infrastructure: locates the reference tree)
+
+REF = oracle.reference_tree()
 
 TU = r'''
 #include "lbm_b200.hpp"
@@ -33,7 +39,7 @@ int main(int argc, char** argv) {
 '''
 
 
-@pytest.mark.skipif(not REF.exists() or shutil.which("g++") is None,
+@pytest.mark.skipif(REF is None or shutil.which("g++") is None,
                     reason="reference tree or g++ not available")
 @pytest.mark.parametrize("double", [False, True])
 def test_reference_consumers_compile_against_wrapper(tmp_path, double, orc):

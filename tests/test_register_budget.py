@@ -30,6 +30,11 @@ DEFAULTS = [
     ("solver.cu", "ring_step_kernel<__nv_bfloat16, FastPhys, 0, 8, 4, 2, 2>", 9, 2),
     ("batch.cu", "batch_ring_kernel<float, ExactPhys<ExactF32>, 4, 2, 4>", 6, 5),
     ("batch.cu", "batch_ring_kernel<__half, FastPhys, 4, 2, 4>", 6, 4),
+    # FP64 ring shapes at the most blocks per SM the autotuner tries (batch_ring_tune_blocks)
+    ("batch.cu", "batch_ring_kernel<double, ExactPhys<ExactF64>, 8, 2, 2>", 9, 2),
+    ("batch.cu", "batch_ring_kernel<double, ExactPhys<ExactF64>, 4, 2, 4>", 5, 4),
+    ("batch.cu", "batch_ring_kernel<double, ExactPhys<ExactF64>, 4, 1, 4>", 5, 4),
+    ("batch.cu", "batch_ring_kernel<double, ExactPhys<ExactF64>, 2, 2, 4>", 3, 6),
     ("adjoint.cu", "adj_forward_kernel<ExactF32, 2, 3, 3>", 9, 3),
     ("adjoint.cu", "adj_backward_kernel<float, 1, 3, 3>", 9, 3),
 ]

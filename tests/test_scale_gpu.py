@@ -71,3 +71,29 @@ def test_launch_shapes_agree_at_scale(gpu_lib, orc):
             s.run(50)
             digests.add(digest(s.populations()))
     assert len(digests) == 1
+
+
+def _wake_hashes():
+    import json
+    from pathlib import Path
+    return json.loads((Path(__file__).resolve().parent / "golden" / "wake_hashes.json").read_text())
+
+
+@pytest.mark.parametrize("real", ["f32", "f64"])
+def test_cylinder_wake_matches_reference_digest(gpu_lib, real):
+    """The cylinder-wake workload (walled 1024 x 256, disc D = 32 at (256, 129), tau 0.548,
+    calibrated force, start u = (0.05, 0)) after 200k steps: plain FP32 and FP64 equal the
+    reference v1 (bitwise v0) run, digests in tests/golden/wake_hashes.json."""
+    h = _wake_hashes()[f"wake_{real}"]
+    solid, _ = gpu_lib.wake.geometry()
+    assert hashlib.sha256(solid.tobytes()).hexdigest() == h["mask_sha"]
+    with gpu_lib.Solver(h["nx"], h["ny"], h["tau"], h["fx"], h["fy"], solid,
+                        precision=PREC[real]) as s:
+        s.init_equilibrium(*h["init"])
+        s.run(h["steps"])
+        rho, ux, uy = s.macroscopic()
+        assert digest(rho) == h["rho"]
+        assert digest(ux) == h["ux"]
+        assert digest(uy) == h["uy"]
+        assert digest(s.populations()) == h["s"]
+        assert s.total_mass() == pytest.approx(h["mass"], rel=1e-12)

@@ -39,3 +39,44 @@ def test_wake_fp16_tracks_fp32(gpu_lib):
     assert 0.20 < ra["st"] < 0.25
     assert rb["st"] == pytest.approx(ra["st"], rel=0.02)
     assert rb["drag_mean"] == pytest.approx(ra["drag_mean"], rel=0.03)
+
+
+def _probe_dir(tmp_path, period, steps=160_000, every=50, amp=0.03, d=40, u=0.05, phase=0.3):
+    step = np.arange(every, steps + 1, every)
+    uy = amp * np.sin(2 * np.pi * step / period + phase) + 0.001
+    lines = ["step,ux,uy,rho"] + [f"{s},0.05,{float(v)!r},1.0" for s, v in zip(step, uy)]
+    (tmp_path / "probe.csv").write_text("\n".join(lines) + "\n")
+    (tmp_path / "meta.json").write_text(
+        f'{{"version": "b200", "case": "cylinder", "nx": 1000, "ny": 320, "tau": 0.56, '
+        f'"u_in": {u}, "re": 100, "diameter": {d}, "steps": {steps}, "real": "float"}}')
+    return tmp_path
+
+
+@pytest.mark.parametrize("period", [4428.0, 3000.0, 5123.7])
+def test_probe_strouhal_of_a_sine(pkg, tmp_path, period):
+    r = pkg.wake.probe_strouhal(_probe_dir(tmp_path, period), start=0.55)
+    assert r["st_fft"] == pytest.approx(40 / period / 0.05, rel=2e-3)
+    assert r["st_zero_crossing"] == pytest.approx(40 / period / 0.05, rel=2e-3)
+    assert r["window_start"] == 88000
+
+
+def test_probe_strouhal_agrees_with_reference_script(pkg, orc, tmp_path):
+    """The restated analysis against the reference's own scripts/strouhal.py on the same
+    probe file (CPU; needs the reference tree)."""
+    import subprocess
+    import sys
+
+    script = orc.REFERENCE_DIR / "scripts" / "strouhal.py"
+    if not script.exists():
+        pytest.skip("reference scripts/strouhal.py not present")
+    d = _probe_dir(tmp_path, 4431.3)
+    r = subprocess.run([sys.executable, str(script), str(d), "--from", "0.55", "--csv",
+                        str(tmp_path / "st.csv")], capture_output=True, text=True)
+    row = (tmp_path / "st.csv").read_text().splitlines()[1].split(",")
+    head = (tmp_path / "st.csv").read_text().splitlines()[0].split(",")
+    ref = dict(zip(head, row))
+    got = pkg.wake.probe_strouhal(d, start=0.55)
+    assert f"{got['st_fft']:.4f}" == ref["st_fft"], r.stdout
+    assert f"{got['st_zero_crossing']:.4f}" == ref["st_zero_crossing"]
+    assert got["periods"] == int(ref["periods"])
+    assert f"{got['uy_amplitude']:.5f}" == ref["uy_amplitude"]

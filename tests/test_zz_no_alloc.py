@@ -7,7 +7,9 @@ on the caller's side) and the population state is the solver's own, reached thro
 lbm_state_view. The entry point is called through the C ABI, twice in a row on the same state
 and once more after further steps, and each result is checked against lbm_total_mass within
 the relative tolerance the other mass checks use (1e-12: the two reductions add the same values
-in different orders). The file is named to be collected last.
+in different orders). The device's free memory (cudaMemGetInfo) is the same before and after
+every call that follows the first, which loads the library's kernels and its static scratch.
+The file is named to be collected last.
 """
 from __future__ import annotations
 
@@ -46,24 +48,31 @@ def test_noalloc_mass_matches_total_mass(gpu_lib, orc, precision):
     with pkg.Solver(nx, ny, 0.7, 2e-6, 0.0, mask, precision=precision) as s:
         s.set_populations(s0)
         s.run(25)
-        for _ in range(2):  # two calls in a row on the same state
+        for call in range(2):  # two calls in a row on the same state
             want = s.total_mass()
             state, plane, pitch = C.c_void_p(), C.c_longlong(), C.c_int()
             assert lib.lbm_state_view(s.handle, C.byref(state), C.byref(plane), C.byref(pitch)) == 0
+            torch.cuda.synchronize()
+            free_before = torch.cuda.mem_get_info()[0]
             rc, msg = _noalloc(lib, state, pkg.PRECISIONS[precision], nx, ny, pitch.value,
                                plane.value, C.c_void_p(solid_dev.data_ptr()),
                                C.c_void_p(out_dev.data_ptr()))
             assert rc == 0, msg
             torch.cuda.synchronize()
+            if call > 0:
+                assert torch.cuda.mem_get_info()[0] == free_before
             assert out_dev.item() == pytest.approx(want, rel=REL)
         s.run(40)  # the scratch keeps the last call's rows; a new state must not see them
         want = s.total_mass()
         assert lib.lbm_state_view(s.handle, C.byref(state), C.byref(plane), C.byref(pitch)) == 0
+        torch.cuda.synchronize()
+        free_before = torch.cuda.mem_get_info()[0]
         rc, msg = _noalloc(lib, state, pkg.PRECISIONS[precision], nx, ny, pitch.value,
                            plane.value, C.c_void_p(solid_dev.data_ptr()),
                            C.c_void_p(out_dev.data_ptr()))
         assert rc == 0, msg
         torch.cuda.synchronize()
+        assert torch.cuda.mem_get_info()[0] == free_before
         assert out_dev.item() == pytest.approx(want, rel=REL)
 
 
