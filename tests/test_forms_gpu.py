@@ -144,3 +144,18 @@ def test_pinned_host_buffers_equal_pageable(gpu_lib, orc, form):
             assert np.array_equal(got.numpy(), w)
         a.populations(pops.numpy())
         assert np.array_equal(pops.numpy(), b.populations())
+
+
+def test_fp16_saturation_is_reported(gpu_lib):
+    """A step whose results exceed the FP16 range (2^15 g_i > 65504) stores them saturated at
+    the largest finite value (cvt.rs.satfinite), and lbm_check_finite reports that as
+    non-finite; the same state stays finite in FP32 and BF16."""
+    nx, ny = 64, 32
+    mask = gpu_lib.make_channel(nx, ny)
+    st = np.where(np.repeat(mask == 0, 9), np.float32(1.99), np.float32(0.0)).astype(np.float32)
+    for form, finite in (("fp16", False), ("bf16", True), ("fp32", True)):
+        with gpu_lib.Solver(nx, ny, 0.8, 0.0, 0.0, mask, precision=form) as s:
+            s.set_populations(st)
+            assert s.check_finite()  # 1.99 * 2^15 fits FP16
+            s.run(1)  # rest population: 1.99 + 1.25 (4/9 * 17.9 - 1.99) ~ 9.5
+            assert s.check_finite() == finite, form
