@@ -819,6 +819,23 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def run_reference_gpu_only(args):
+    """Only the reference's own GPU kernel on the headline grid and seeded state (`--warmup`
+    steps, then one timed_run of `--steps` steps): the command its ncu profile is taken with."""
+    import __graft_entry__ as entry
+    pkg = entry.package()
+    orc = entry.oracle_module()
+    n = args.nx
+    real = "f64" if args.precision == "fp64" else "f32"
+    mask = pkg.make_channel(n, n)
+    s0 = pkg.workloads.seeded_state(SEED, AMP, n, n, mask, np.float64 if real == "f64" else np.float32)
+    secs, info, _ = orc.ReferenceV3(real).bench(n, n, mask, TAU, FX, FY, s0, args.steps,
+                                                warmup=args.warmup, reps=1)
+    print(json.dumps({"impl": "reference_v3_gpu", "nx": n, "ny": n, "real": real,
+                      "steps": args.steps, "mlups": round(n * n * args.steps / secs[0] / 1e6, 1),
+                      "bench_info": info}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser(description=__doc__,
                                  formatter_class=argparse.RawDescriptionHelpFormatter)
@@ -852,10 +869,14 @@ def main():
                     help="skip timing the reference's own GPU kernel")
     ap.add_argument("--reps", type=int, default=5,
                     help="repetitions the K timed steps of the headline are split into")
+    ap.add_argument("--profile-reference-gpu", action="store_true",
+                    help="run only the reference's own GPU kernel (for its ncu profile)")
     args = ap.parse_args()
     if args.steps < 1:
         ap.error("--steps must be >= 1")
-    if args.impl == "reference":
+    if args.profile_reference_gpu:
+        run_reference_gpu_only(args)
+    elif args.impl == "reference":
         run_reference(args)
     else:
         run_ours(args)

@@ -311,21 +311,15 @@ __device__ __forceinline__ void store_vec<__nv_bfloat16>(__nv_bfloat16* p, const
 // plus r are truncated (round toward zero), which rounds up with probability equal to the
 // dropped fraction, so E[stored] = v and sub-ulp increments survive on average.
 //
-// Blackwell does this in one instruction per pair of values: cvt.rs.satfinite.{f16x2,bf16x2}.f32
-// takes 32 random bits and adds them below the kept significand of each value before
-// truncating. An in-bounds probe on a GB300 (single set bits, and the mean over 10^6 random
-// words) showed which bits each half uses and that the result is unbiased: FP16 takes bits
-// [0, 13) for the low half and [16, 29) for the high half, BF16 bits [0, 16) and [16, 32); all
-// random bits zero is plain truncation. .satfinite clamps a value past the format's largest
-// finite value to it (the finite check treats a saturated value as diverged).
-//
-// The random bits of each value are a deterministic function of (cell pair, plane, step): a
+// The D random bits of each value are a deterministic function of (cell pair, plane, step): a
 // 32-bit hash H of the pair's cell offset (y * pitch + x) / 2 xor the step key, rotated left by
-// 7 i bits for plane i, gives the conversion's 32 random bits; the two halves read disjoint
-// fields, each uniform because H is. Fields of different planes overlap, so their rounding
-// errors are correlated, which leaves every stored value unbiased. Every kernel variant derives
-// them identically, so results do not depend on the variant, and a run is reproducible from its
-// step counter. The hash is the "lowbias32" integer mixer (C. Wellons, hash-prospector, 2018).
+// 7 i bits for plane i; bits [32 - D, 32) of the rotation go to the pair's even cell and bits
+// [0, D) to its odd cell (D <= 16: disjoint fields, each uniform because H is). Fields of
+// different planes overlap, so their rounding errors are correlated, which leaves every stored
+// value unbiased. Integer rotations and masks keep this off the FP32 pipes. Every kernel variant derives them identically, so results do not depend on
+// the variant, and a run is reproducible from its step counter. The hash is the "lowbias32"
+// integer mixer (C. Wellons, hash-prospector, 2018). Values past the format's largest finite
+// value saturate (round toward zero); the finite check treats a saturated value as diverged.
 // ---------------------------------------------------------------------------------------------
 __host__ __device__ constexpr uint32_t mix32(uint32_t x) {
   x ^= x >> 16;
@@ -344,19 +338,29 @@ __device__ __forceinline__ uint32_t sr_pair_hash(long long cell, uint32_t rkey) 
   return mix32(static_cast<uint32_t>(cell >> 1) ^ rkey);
 }
 
-// Stochastically rounded, saturating conversion of a pair (lo = even cell, in the low half).
 template <class ST>
-__device__ __forceinline__ uint32_t cvt_rs_pair(float lo, float hi, uint32_t rbits);
+struct SrFormat;
 template <>
-__device__ __forceinline__ uint32_t cvt_rs_pair<__half>(float lo, float hi, uint32_t rbits) {
+struct SrFormat<__half> {
+  static constexpr int kDrop = 13;
+};
+template <>
+struct SrFormat<__nv_bfloat16> {
+  static constexpr int kDrop = 16;
+};
+
+template <class ST>
+__device__ __forceinline__ uint32_t cvt_rz_pair(float lo, float hi);
+template <>
+__device__ __forceinline__ uint32_t cvt_rz_pair<__half>(float lo, float hi) {
   uint32_t d;
-  asm("cvt.rs.satfinite.f16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+  asm("cvt.rz.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
   return d;
 }
 template <>
-__device__ __forceinline__ uint32_t cvt_rs_pair<__nv_bfloat16>(float lo, float hi, uint32_t rbits) {
+__device__ __forceinline__ uint32_t cvt_rz_pair<__nv_bfloat16>(float lo, float hi) {
   uint32_t d;
-  asm("cvt.rs.satfinite.bf16x2.f32 %0, %1, %2, %3;" : "=r"(d) : "f"(hi), "f"(lo), "r"(rbits));
+  asm("cvt.rz.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(hi), "f"(lo));
   return d;
 }
 
@@ -364,7 +368,13 @@ __device__ __forceinline__ uint32_t cvt_rs_pair<__nv_bfloat16>(float lo, float h
 // half).
 template <class ST>
 __device__ __forceinline__ uint32_t encode_pair_sr(float lo, float hi, int i, uint32_t pair_hash) {
-  return cvt_rs_pair<ST>(lo, hi, __funnelshift_l(pair_hash, pair_hash, sr_plane_rot(i)));
+  constexpr int D = SrFormat<ST>::kDrop;
+  const uint32_t h = __funnelshift_l(pair_hash, pair_hash, sr_plane_rot(i));
+  const uint32_t r0 = h >> (32 - D);
+  const uint32_t r1 = h & ((1u << D) - 1u);
+  const float a = __uint_as_float(__float_as_uint(lo) + r0);
+  const float b = __uint_as_float(__float_as_uint(hi) + r1);
+  return cvt_rz_pair<ST>(a, b);
 }
 
 // True for a stored 16-bit value at the format's largest finite magnitude (saturated).

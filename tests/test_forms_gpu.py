@@ -148,8 +148,8 @@ def test_pinned_host_buffers_equal_pageable(gpu_lib, orc, form):
 
 def test_fp16_saturation_is_reported(gpu_lib):
     """A step whose results exceed the FP16 range (2^15 g_i > 65504) stores them saturated at
-    the largest finite value (cvt.rs.satfinite), and lbm_check_finite reports that as
-    non-finite; the same state stays finite in FP32 and BF16."""
+    the largest finite value (the stochastic rounding truncates toward zero), and
+    lbm_check_finite reports that as non-finite; the same state stays finite in FP32 and BF16."""
     nx, ny = 64, 32
     mask = gpu_lib.make_channel(nx, ny)
     st = np.where(np.repeat(mask == 0, 9), np.float32(1.99), np.float32(0.0)).astype(np.float32)
