@@ -7,8 +7,9 @@
 // instance by binary search over the first-chunk indices staged in shared memory, and run the
 // same chunk code as the single-grid kernel (step_kernel.cuh). The default kernel is instead the
 // warp-specialised ring of the single-grid solver (step_ring.cuh) over the ensemble's tiles of
-// consecutive row strips (a tile may cover several short rows): a tile's instance comes from a
-// binary search over the per-instance first-tile indices staged in shared memory. Steps are replayed from a CUDA graph of kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
+// consecutive row strips (a tile may cover several short rows): a tile's instance and place come
+// from a per-tile header built on the host (TileHead). Steps are replayed from a CUDA graph of
+// kGraphSteps launches. lbm_batch_run_separate() runs the same instances one launch per
 // instance per step (the comparison point). lbm_batch_autotune() times the candidate launch
 // shapes (cells per thread G, i.e. the chunk width 32 G, threads per block, blocks per SM) on the
 // actual ensemble and keeps the fastest, caching the choice per GPU, form and ensemble size.
@@ -64,6 +65,16 @@ struct alignas(16) StagedArgs {
   StepArgs<ST, Phys> p;
 };
 
+// Where a ring tile lies, built on the host with the table (one per tile): it spares every
+// producer a search over the instances and the divisions that locate a tile.
+//   inst_nseg  instance index | (row segments of a strip tile << 16) (0 segments: whole rows);
+//   ya         the tile's first row;
+//   a, b       whole-row tiles: rows in the tile, 0; strip tiles: first strip and one past the
+//              last (strips numbered row by row within the instance).
+struct alignas(16) TileHead {
+  int inst_nseg, ya, a, b;
+};
+
 template <class ST, class Phys>
 struct BatchArgs {
   const ST* src;
@@ -77,6 +88,7 @@ struct BatchArgs {
   const StagedArgs<ST, Phys>* args;  // [instance][parity]
   int parity;                        // src == buffer `parity`; odd parity walks the tiles backwards
   int tiles;                         // ring tiles of the ensemble
+  const TileHead* heads;             // [tiles]
 };
 
 // Device step counter of a batch: read by every step launch, advanced by one after it (inside a
@@ -199,19 +211,6 @@ struct BatchFlatPolicy {
   static constexpr int kStageBytes = kDescOff + kW * static_cast<int>(sizeof(StripDesc));
   static_assert(kArgsBytes % 16 == 0, "step arguments are copied in 16-byte units");
   const BatchArgs<ST, Phys>& a;
-  const int* s_tile0;
-
-  __device__ __forceinline__ int instance_of(int tile) const {
-    int lo = 0, hi = a.count - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (s_tile0[mid] <= tile)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    return lo;
-  }
 
   __device__ __forceinline__ StepArgs<ST, Phys> grid_of(const Inst& d) const {
     StepArgs<ST, Phys> p;
@@ -303,24 +302,29 @@ struct BatchFlatPolicy {
     return S::MW * 4;
   }
 
-  // Producer (all 32 lanes): the lanes describe the consumer warps' strips and size the tile's
-  // copies; lane 0 arms the stage's barrier with the byte count; then the lanes issue the copies
-  // between them (strip tiles: 18 per segment, those that apply; whole-row tiles: at most
-  // 2 per plane and one per mask row) and lane 0 the step arguments' copy.
+  // Producer (all 32 lanes): the lanes describe the consumer warps' strips, lane 0 copies the
+  // step arguments, the lanes issue the data copies between them (strip tiles: 18 per segment,
+  // those that apply; whole-row tiles: at most 2 per plane and one per mask row), adding up their
+  // bytes, and lane 0 then arrives on the stage's barrier with the byte count. A copy may land
+  // before that arrive: its complete-tx takes the barrier's transaction count below zero, which
+  // the barrier allows, and the phase cannot complete before the arrive (one expected arrival).
+  // Sizing the copies as they are issued, instead of in a pass of their own, and reading the
+  // tile's place from its TileHead, keep the producer's instructions, which compete with the
+  // consumers' for issue slots, to about half.
   __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
     // Odd steps walk the tiles from the last: they start on the rows the previous step wrote
     // last, still in L2 (the consumers only read what the producer staged).
     if (a.parity) tile = a.tiles - 1 - tile;
-    const int k = instance_of(tile);
+    const TileHead h = a.heads[tile];
+    const int k = h.inst_nseg & 0xffff;
     const Inst& d = a.inst[k];
     const StepArgs<ST, Phys> p = grid_of(d);
     const int ny = d.g.ny;
     uint32_t bytes = 0;
     StripDesc sd;
     if (d.rpt) {
-      const int ya = (tile - s_tile0[k]) * d.rpt;
-      const int rn = d.rpt < ny - ya ? d.rpt : ny - ya;
-      if (lane < 2 * kQ + rn + 2) bytes = row_copy(p, base, full, ya, rn, lane, false);
+      const int ya = h.ya;
+      const int rn = h.a;
       const int r = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(lane)));
       const int j = lane - r * d.spr;
       sd.flags = (r < rn ? kStripValid : 0) | kStripRows;
@@ -330,31 +334,20 @@ struct BatchFlatPolicy {
       sd.w0 = sd.x0 >> 5;
       sd.sm_off = r * S::MW;
       sd.wr_off = 0;
-      bytes = __reduce_add_sync(0xffffffffu, bytes);
       if (lane < kW) {
         sd.ym = sd.y == 0 ? ny - 1 : sd.y - 1;
         sd.yp = sd.y == ny - 1 ? 0 : sd.y + 1;
         reinterpret_cast<StripDesc*>(base + kDescOff)[lane] = sd;
       }
       __syncwarp();
-      if (lane == 0) {
-        mbar_arrive_expect_tx(full, bytes + kArgsBytes);
-        bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
-      }
-      __syncwarp();
-      if (lane < 2 * kQ + rn + 2) row_copy(p, base, full, ya, rn, lane, true);
+      if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
+      if (lane < 2 * kQ + rn + 2) bytes = row_copy(p, base, full, ya, rn, lane, true);
+      bytes = __reduce_add_sync(0xffffffffu, bytes);
+      if (lane == 0) mbar_arrive_expect_tx(full, bytes + kArgsBytes);
       return;
     }
-    const int strips = d.spr * ny;
-    const int s0 = (tile - s_tile0[k]) * kW;
-    const int s1 = s0 + kW < strips ? s0 + kW : strips;
-    const int ya = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s0)));
-    const int nseg = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(s1 - 1))) - ya + 1;
-    for (int c = lane; c < nseg * 18; c += 32) {
-      const int g = c / 18;
-      bytes += copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, false);
-    }
-    bytes = __reduce_add_sync(0xffffffffu, bytes);
+    const int s0 = h.a, s1 = h.b, ya = h.ya;
+    const int nseg = h.inst_nseg >> 16;
     if (lane < kW) {
       // Lane w describes consumer warp w's strip (ordered before lane 0's arrive by __syncwarp;
       // the consumers acquire it with the barrier phase).
@@ -375,13 +368,13 @@ struct BatchFlatPolicy {
       reinterpret_cast<StripDesc*>(base + kDescOff)[lane] = sd;
     }
     __syncwarp();
-    if (lane == 0) mbar_arrive_expect_tx(full, bytes + kArgsBytes);
-    __syncwarp();
     if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
     for (int c = lane; c < nseg * 18; c += 32) {
       const int g = c / 18;
-      copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, true);
+      bytes += copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, true);
     }
+    bytes = __reduce_add_sync(0xffffffffu, bytes);
+    if (lane == 0) mbar_arrive_expect_tx(full, bytes + kArgsBytes);
   }
 
   template <bool kRows>
@@ -420,8 +413,7 @@ struct BatchFlatPolicy {
   __device__ __forceinline__ void finish(int, int) const {}
 };
 
-// Shared memory of a batch ring block before the staged first-tile indices: the stages and the
-// ring's barriers.
+// Shared memory of a batch ring block: the stages and the ring's barriers.
 template <class Pol>
 __host__ __device__ constexpr size_t batch_ring_smem(int stages) {
   return static_cast<size_t>(stages) * Pol::kStageBytes + 2 * stages * sizeof(uint64_t);
@@ -451,10 +443,7 @@ __global__ void __launch_bounds__(FlatShape<ST, kW, kC>::kThreads, (batch_ring_m
     batch_ring_kernel(const BatchArgs<ST, Phys> a, int tiles, int* err) {
   using Pol = BatchFlatPolicy<ST, Phys, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
-  int* s_tile0 = reinterpret_cast<int*>(smem + batch_ring_smem<Pol>(kStages));
-  for (int k = threadIdx.x; k < a.count; k += blockDim.x) s_tile0[k] = a.inst[k].tile0;
-  __syncthreads();
-  Pol pol{a, s_tile0};
+  Pol pol{a};
   tile_pipeline<kW, kStages, Pol::kStageBytes, FlatShape<ST, kW, kC>::kProd>(smem, pol, tiles, err);
 }
 
@@ -506,6 +495,8 @@ struct lbm_batch {
   uint32_t* mask_d = nullptr;
   void* table_d = nullptr;  // BatchInst<Consts>[count] for the current G
   void* args_d = nullptr;   // StagedArgs[count][2] (step arguments per instance and parity)
+  void* heads_d = nullptr;  // TileHead[heads_cap] of the ring tiles of the table
+  int heads_cap = 0;
   int table_G = 0;
   void* stage = nullptr;
   size_t stage_bytes = 0;
@@ -577,6 +568,36 @@ int build_table(lbm_batch* b, int G) {
                   : static_cast<int>((static_cast<long long>(d.spr) * in.ny + b->table_kw - 1) / b->table_kw);
   }
   b->tiles = tile;
+  // Tile headers of the ring kernel (the producers' decode of a tile, done once here).
+  std::vector<TileHead> heads(tile > 0 ? tile : 1);
+  for (int k = 0; k < b->count; ++k) {
+    const BatchInst<Consts>& d = tab[k];
+    const int ny = d.g.ny, kw = b->table_kw;
+    const int n = (k + 1 < b->count ? tab[k + 1].tile0 : tile) - d.tile0;
+    for (int j = 0; j < n; ++j) {
+      TileHead& h = heads[d.tile0 + j];
+      if (d.rpt) {
+        h.ya = j * d.rpt;
+        h.a = std::min(d.rpt, ny - h.ya);
+        h.b = 0;
+        h.inst_nseg = k;
+      } else {
+        const int strips = d.spr * ny;
+        h.a = j * kw;
+        h.b = std::min(h.a + kw, strips);
+        h.ya = h.a / d.spr;
+        h.inst_nseg = k | (((h.b - 1) / d.spr - h.ya + 1) << 16);
+      }
+    }
+  }
+  if (b->heads_cap < static_cast<int>(heads.size())) {
+    cudaFree(b->heads_d);
+    b->heads_d = nullptr;
+    b->heads_cap = 0;
+    B_CUDA(b, cudaMalloc(&b->heads_d, heads.size() * sizeof(TileHead)));
+    b->heads_cap = static_cast<int>(heads.size());
+  }
+  B_CUDA(b, cudaMemcpy(b->heads_d, heads.data(), heads.size() * sizeof(TileHead), cudaMemcpyHostToDevice));
   using Phys = typename BForm<ST>::Phys;
   std::vector<StagedArgs<ST, Phys>> args(2 * static_cast<size_t>(b->count));
   for (int k = 0; k < b->count; ++k) {
@@ -652,8 +673,7 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
   using Phys = typename BForm<ST>::Phys;
   using S = FlatShape<ST, kW, kC>;
   const auto kernel = batch_ring_kernel<ST, Phys, kW, kC, kStages>;
-  const size_t smem = batch_ring_smem<BatchFlatPolicy<ST, Phys, kW, kC>>(kStages) +
-                      static_cast<size_t>(b->count) * sizeof(int);
+  const size_t smem = batch_ring_smem<BatchFlatPolicy<ST, Phys, kW, kC>>(kStages);
   if (prepare_only) {
     if (b->table_G == 0 || b->table_sw != S::SW || b->table_kw != kW) {
       b->table_sw = S::SW;
@@ -679,6 +699,7 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
   a.step = b->step_d;
   a.args = static_cast<const StagedArgs<ST, Phys>*>(b->args_d);
   a.tiles = b->tiles;
+  a.heads = static_cast<const TileHead*>(b->heads_d);
   int* err = reinterpret_cast<int*>(b->step_d + 1);
   for (int s = 0; s < steps; ++s) {
     a.src = static_cast<const ST*>(b->buf[b->cur]);
@@ -1029,7 +1050,7 @@ int lbm_batch_destroy(lbm_batch* b) {
   if (!b) return LBM_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->args_d, b->stage,
+  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->args_d, b->heads_d, b->stage,
                   static_cast<void*>(b->red), static_cast<void*>(b->step_d)})
     cudaFree(p);
   for (cudaEvent_t ev : b->ev)
