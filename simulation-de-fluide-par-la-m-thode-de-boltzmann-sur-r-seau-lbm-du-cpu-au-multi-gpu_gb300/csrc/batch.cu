@@ -65,15 +65,31 @@ struct alignas(16) StagedArgs {
   StepArgs<ST, Phys> p;
 };
 
-// Where a ring tile lies, built on the host with the table (one per tile): it spares every
-// producer a search over the instances and the divisions that locate a tile.
+// The copy plan of the ring tiles, built on the host for the current tile shape (build_plan):
+// the producer warps read where a tile lies and which bulk copies fill its stage instead of
+// deriving them, so that their instructions, which compete with the consumers' for issue
+// slots, stay few.
+//
+// Per tile (TilePlan):
 //   inst_nseg  instance index | (row segments of a strip tile << 16) (0 segments: whole rows);
 //   ya         the tile's first row;
 //   a, b       whole-row tiles: rows in the tile, 0; strip tiles: first strip and one past the
-//              last (strips numbered row by row within the instance).
-struct alignas(16) TileHead {
+//              last (strips numbered row by row within the instance);
+//   first, ncopy, bytes  its copies in the copy array and their total size.
+// Per copy (CopyOp, 8 bytes): source offset in 16-byte units from the state buffer being read,
+// or from the mask buffer (bit 15 of len16), destination offset and length in 16-byte units
+// within the stage.
+struct alignas(16) TilePlan {
   int inst_nseg, ya, a, b;
+  int first, ncopy, bytes, pad;
 };
+struct CopyOp {
+  uint32_t src16;
+  uint16_t dst16;
+  uint16_t len16;
+};
+static_assert(sizeof(CopyOp) == 8, "copy descriptors are 8 bytes");
+constexpr uint16_t kCopyFromMask = 0x8000u;
 
 template <class ST, class Phys>
 struct BatchArgs {
@@ -88,7 +104,8 @@ struct BatchArgs {
   const StagedArgs<ST, Phys>* args;  // [instance][parity]
   int parity;                        // src == buffer `parity`; odd parity walks the tiles backwards
   int tiles;                         // ring tiles of the ensemble
-  const TileHead* heads;             // [tiles]
+  const TilePlan* plans;             // [tiles]
+  const CopyOp* ops;                 // the tiles' copies
 };
 
 // Device step counter of a batch: read by every step launch, advanced by one after it (inside a
@@ -176,7 +193,7 @@ struct FlatShape {
 struct Segment {
   int y, j_lo, j_hi, w_first;
 };
-__device__ __forceinline__ Segment tile_segment(int g, int s0, int s1, int ya, int spr) {
+inline Segment tile_segment(int g, int s0, int s1, int ya, int spr) {
   Segment sg;
   sg.y = ya + g;
   const int row_s = sg.y * spr;
@@ -212,119 +229,22 @@ struct BatchFlatPolicy {
   static_assert(kArgsBytes % 16 == 0, "step arguments are copied in 16-byte units");
   const BatchArgs<ST, Phys>& a;
 
-  __device__ __forceinline__ StepArgs<ST, Phys> grid_of(const Inst& d) const {
-    StepArgs<ST, Phys> p;
-    p.src = a.src + d.off;
-    p.dst = a.dst + d.off;
-    p.mask = a.mask + d.mask_off;
-    p.g = d.g;
-    p.k = d.k;
-    p.sc = a.sc;
-    p.step_ctr = a.step;
-    p.step_off = 0;
-    p.key_base = d.off / kQ;
-    return p;
-  }
-
-  // Copy q (0 .. 17) of segment g: 0..8 plane rows, 9..11 mask rows, 12..14 the wrap blocks of
-  // column nx - 1 (planes 1, 5, 8; segment starting at x = 0), 15..17 those of column 0 (planes
-  // 3, 6, 7; segment ending at x = nx - 1). Returns its byte count (0: not needed) and issues it
-  // when `go`.
-  __device__ __forceinline__ uint32_t copy(const StepArgs<ST, Phys>& p, unsigned char* base, uint64_t* full,
-                                           const Segment& sg, int g, int q, bool go) const {
-    const int nx = p.g.nx, ny = p.g.ny, spr = (nx + S::SW - 1) / S::SW;
-    const int y = sg.y;
-    const int ym = y == 0 ? ny - 1 : y - 1;
-    const int yp = y == ny - 1 ? 0 : y + 1;
-    if (q < kQ) {
-      const int x0 = sg.j_lo * S::SW;
-      const int xs = x0 - S::H > 0 ? x0 - S::H : 0;
-      const int xe0 = (sg.j_hi + 1) * S::SW + S::H;
-      const int xe = xe0 < p.g.pitch ? xe0 : p.g.pitch;
-      const uint32_t bytes = static_cast<uint32_t>((xe - xs) * sizeof(ST));
-      if (go) {
-        ST* dst = reinterpret_cast<ST*>(base) + q * S::SROW + sg.w_first * S::SW + 2 * g * S::H + (xs - (x0 - S::H));
-        bulk_copy_g2s(dst, p.src + q * p.g.plane + static_cast<long long>(src_row(q, y, ym, yp)) * p.g.pitch + xs,
-                      bytes, full);
-      }
-      return bytes;
-    }
-    if (q < kQ + 3) {
-      const int r = q - kQ;
-      const int row = r == 0 ? ym : (r == 1 ? y : yp);
-      if (go) {
-        uint32_t* sm = reinterpret_cast<uint32_t*>(base + S::kPlaneBytes) + (g * 3 + r) * S::MW;
-        bulk_copy_g2s(sm, p.mask + static_cast<size_t>(row) * p.g.mask_words + (((sg.j_lo * S::SW) >> 5) & ~3),
-                      S::MW * 4, full);
-      }
-      return S::MW * 4;
-    }
-    const int wj = q - kQ - 3;  // wrap block 0..5
-    const bool lo = wj < 3;
-    if (lo ? sg.j_lo != 0 : sg.j_hi != spr - 1) return 0;
-    const int i = wrap_dir(wj);
-    if (go) {
-      ST* wr = reinterpret_cast<ST*>(base + S::kPlaneBytes + S::kMaskBytes) + (g * 6 + wj) * S::H;
-      const int xb = lo ? ((nx - 1) & ~(S::H - 1)) : 0;
-      bulk_copy_g2s(wr, p.src + i * p.g.plane + static_cast<long long>(src_row(i, y, ym, yp)) * p.g.pitch + xb, 16,
-                    full);
-    }
-    return 16;
-  }
-
-  // Copy c of a whole-row tile (rows ya .. ya + rn - 1): c < 18 plane i = c / 2 rows ya - c_y ..,
-  // split where they wrap past row ny - 1 (run c % 2), one copy per run into plane i's stage rows
-  // at pitch stride; 18 .. 18 + rn + 1: mask row ya - 1 + (c - 18), words 0 .. MW - 1.
-  __device__ __forceinline__ uint32_t row_copy(const StepArgs<ST, Phys>& p, unsigned char* base, uint64_t* full,
-                                               int ya, int rn, int c, bool go) const {
-    const int ny = p.g.ny, pitch = p.g.pitch;
-    if (c < 2 * kQ) {
-      const int i = c >> 1;
-      int r0 = ya - dir_cy(i);
-      r0 = r0 < 0 ? r0 + ny : (r0 >= ny ? r0 - ny : r0);
-      const int len0 = rn < ny - r0 ? rn : ny - r0;
-      const int rs = (c & 1) ? 0 : r0;
-      const int len = (c & 1) ? rn - len0 : len0;
-      if (len <= 0) return 0;
-      const uint32_t bytes = static_cast<uint32_t>(len) * pitch * sizeof(ST);
-      if (go)
-        bulk_copy_g2s(reinterpret_cast<ST*>(base) + i * S::SROW + ((c & 1) ? len0 : 0) * pitch,
-                      p.src + i * p.g.plane + static_cast<long long>(rs) * pitch, bytes, full);
-      return bytes;
-    }
-    const int k = c - 2 * kQ;
-    if (k >= rn + 2) return 0;
-    int m = ya - 1 + k;
-    m = m < 0 ? m + ny : (m >= ny ? m - ny : m);
-    if (go)
-      bulk_copy_g2s(reinterpret_cast<uint32_t*>(base + S::kPlaneBytes) + k * S::MW,
-                    p.mask + static_cast<size_t>(m) * p.g.mask_words, S::MW * 4, full);
-    return S::MW * 4;
-  }
-
   // Producer (all 32 lanes): the lanes describe the consumer warps' strips, lane 0 copies the
-  // step arguments, the lanes issue the data copies between them (strip tiles: 18 per segment,
-  // those that apply; whole-row tiles: at most 2 per plane and one per mask row), adding up their
-  // bytes, and lane 0 then arrives on the stage's barrier with the byte count. A copy may land
-  // before that arrive: its complete-tx takes the barrier's transaction count below zero, which
-  // the barrier allows, and the phase cannot complete before the arrive (one expected arrival).
-  // Sizing the copies as they are issued, instead of in a pass of their own, and reading the
-  // tile's place from its TileHead, keep the producer's instructions, which compete with the
-  // consumers' for issue slots, to about half.
+  // step arguments, the lanes issue the tile's planned copies between them, and lane 0 then
+  // arrives on the stage's barrier with their byte count. A copy may land before that arrive:
+  // its complete-tx takes the barrier's transaction count below zero, which the barrier allows,
+  // and the phase cannot complete before the arrive (one expected arrival).
   __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
     // Odd steps walk the tiles from the last: they start on the rows the previous step wrote
     // last, still in L2 (the consumers only read what the producer staged).
     if (a.parity) tile = a.tiles - 1 - tile;
-    const TileHead h = a.heads[tile];
+    const TilePlan h = a.plans[tile];
     const int k = h.inst_nseg & 0xffff;
     const Inst& d = a.inst[k];
-    const StepArgs<ST, Phys> p = grid_of(d);
     const int ny = d.g.ny;
-    uint32_t bytes = 0;
     StripDesc sd;
     if (d.rpt) {
-      const int ya = h.ya;
-      const int rn = h.a;
+      const int ya = h.ya, rn = h.a;
       const int r = static_cast<int>(d.spr_div.div(static_cast<uint32_t>(lane)));
       const int j = lane - r * d.spr;
       sd.flags = (r < rn ? kStripValid : 0) | kStripRows;
@@ -334,23 +254,9 @@ struct BatchFlatPolicy {
       sd.w0 = sd.x0 >> 5;
       sd.sm_off = r * S::MW;
       sd.wr_off = 0;
-      if (lane < kW) {
-        sd.ym = sd.y == 0 ? ny - 1 : sd.y - 1;
-        sd.yp = sd.y == ny - 1 ? 0 : sd.y + 1;
-        reinterpret_cast<StripDesc*>(base + kDescOff)[lane] = sd;
-      }
-      __syncwarp();
-      if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
-      if (lane < 2 * kQ + rn + 2) bytes = row_copy(p, base, full, ya, rn, lane, true);
-      bytes = __reduce_add_sync(0xffffffffu, bytes);
-      if (lane == 0) mbar_arrive_expect_tx(full, bytes + kArgsBytes);
-      return;
-    }
-    const int s0 = h.a, s1 = h.b, ya = h.ya;
-    const int nseg = h.inst_nseg >> 16;
-    if (lane < kW) {
-      // Lane w describes consumer warp w's strip (ordered before lane 0's arrive by __syncwarp;
-      // the consumers acquire it with the barrier phase).
+    } else {
+      // Lane w describes consumer warp w's strip.
+      const int s0 = h.a, s1 = h.b, ya = h.ya;
       const int st = s0 + lane;
       const bool valid = st < s1;
       sd.flags = valid ? kStripValid : 0;
@@ -358,23 +264,28 @@ struct BatchFlatPolicy {
       const int j = (valid ? st : s0) - sd.y * d.spr;
       const int g = sd.y - ya;
       const int j_lo = g == 0 ? s0 - ya * d.spr : 0;
-      sd.ym = sd.y == 0 ? ny - 1 : sd.y - 1;
-      sd.yp = sd.y == ny - 1 ? 0 : sd.y + 1;
       sd.x0 = j * S::SW;
       sd.lx0 = lane * S::SW + (2 * g + 1) * S::H;
       sd.w0 = (sd.x0 >> 5) - (((j_lo * S::SW) >> 5) & ~3);
       sd.sm_off = g * 3 * S::MW;
       sd.wr_off = g * 6 * S::H;
+    }
+    if (lane < kW) {
+      // Ordered before lane 0's arrive by __syncwarp; the consumers acquire it with the phase.
+      sd.ym = sd.y == 0 ? ny - 1 : sd.y - 1;
+      sd.yp = sd.y == ny - 1 ? 0 : sd.y + 1;
       reinterpret_cast<StripDesc*>(base + kDescOff)[lane] = sd;
     }
     __syncwarp();
     if (lane == 0) bulk_copy_g2s(base + S::kStageBytes, a.args + 2 * k + a.parity, kArgsBytes, full);
-    for (int c = lane; c < nseg * 18; c += 32) {
-      const int g = c / 18;
-      bytes += copy(p, base, full, tile_segment(g, s0, s1, ya, d.spr), g, c - 18 * g, true);
+    const CopyOp* ops = a.ops + h.first;
+    for (int c = lane; c < h.ncopy; c += 32) {
+      const CopyOp op = ops[c];
+      const unsigned char* src = (op.len16 & kCopyFromMask) ? reinterpret_cast<const unsigned char*>(a.mask)
+                                                             : reinterpret_cast<const unsigned char*>(a.src);
+      bulk_copy_g2s(base + 16u * op.dst16, src + 16ull * op.src16, 16u * (op.len16 & ~kCopyFromMask), full);
     }
-    bytes = __reduce_add_sync(0xffffffffu, bytes);
-    if (lane == 0) mbar_arrive_expect_tx(full, bytes + kArgsBytes);
+    if (lane == 0) mbar_arrive_expect_tx(full, static_cast<uint32_t>(h.bytes) + kArgsBytes);
   }
 
   template <bool kRows>
@@ -495,8 +406,11 @@ struct lbm_batch {
   uint32_t* mask_d = nullptr;
   void* table_d = nullptr;  // BatchInst<Consts>[count] for the current G
   void* args_d = nullptr;   // StagedArgs[count][2] (step arguments per instance and parity)
-  void* heads_d = nullptr;  // TileHead[heads_cap] of the ring tiles of the table
-  int heads_cap = 0;
+  void* plans_d = nullptr;  // TilePlan[plans_cap]: the ring tiles of the current tile shape
+  void* ops_d = nullptr;    // CopyOp[ops_cap]: their copies
+  long long plans_cap = 0, ops_cap = 0;
+  int plan_sw = 0, plan_kw = 0, plan_kc = 0;  // tile shape of the current plan
+  long long mask_words_total = 0;
   int table_G = 0;
   void* stage = nullptr;
   size_t stage_bytes = 0;
@@ -568,36 +482,6 @@ int build_table(lbm_batch* b, int G) {
                   : static_cast<int>((static_cast<long long>(d.spr) * in.ny + b->table_kw - 1) / b->table_kw);
   }
   b->tiles = tile;
-  // Tile headers of the ring kernel (the producers' decode of a tile, done once here).
-  std::vector<TileHead> heads(tile > 0 ? tile : 1);
-  for (int k = 0; k < b->count; ++k) {
-    const BatchInst<Consts>& d = tab[k];
-    const int ny = d.g.ny, kw = b->table_kw;
-    const int n = (k + 1 < b->count ? tab[k + 1].tile0 : tile) - d.tile0;
-    for (int j = 0; j < n; ++j) {
-      TileHead& h = heads[d.tile0 + j];
-      if (d.rpt) {
-        h.ya = j * d.rpt;
-        h.a = std::min(d.rpt, ny - h.ya);
-        h.b = 0;
-        h.inst_nseg = k;
-      } else {
-        const int strips = d.spr * ny;
-        h.a = j * kw;
-        h.b = std::min(h.a + kw, strips);
-        h.ya = h.a / d.spr;
-        h.inst_nseg = k | (((h.b - 1) / d.spr - h.ya + 1) << 16);
-      }
-    }
-  }
-  if (b->heads_cap < static_cast<int>(heads.size())) {
-    cudaFree(b->heads_d);
-    b->heads_d = nullptr;
-    b->heads_cap = 0;
-    B_CUDA(b, cudaMalloc(&b->heads_d, heads.size() * sizeof(TileHead)));
-    b->heads_cap = static_cast<int>(heads.size());
-  }
-  B_CUDA(b, cudaMemcpy(b->heads_d, heads.data(), heads.size() * sizeof(TileHead), cudaMemcpyHostToDevice));
   using Phys = typename BForm<ST>::Phys;
   std::vector<StagedArgs<ST, Phys>> args(2 * static_cast<size_t>(b->count));
   for (int k = 0; k < b->count; ++k) {
@@ -621,6 +505,143 @@ int build_table(lbm_batch* b, int G) {
   B_CUDA(b, cudaMemcpy(b->table_d, tab.data(), b->count * sizeof(BatchInst<Consts>), cudaMemcpyHostToDevice));
   b->items = item;
   b->table_G = G;
+  return LBM_OK;
+}
+
+// Source row of plane i for destination row y (the host's copy of src_row) and the plane of wrap
+// block j (of wrap_dir).
+inline int plan_src_row(int i, int y, int ym, int yp) { return dir_cy(i) == 1 ? ym : (dir_cy(i) == -1 ? yp : y); }
+inline int plan_wrap_dir(int j) { return j == 0 ? 1 : j == 1 ? 5 : j == 2 ? 8 : j == 3 ? 3 : j == 4 ? 6 : 7; }
+
+// Builds the copy plan of the ring tiles for tile shape kW x kC (the table's tiling: whole rows
+// where a row holds at most kW strips, kW consecutive strips otherwise). The copies are those
+// the stage layout of FlatShape needs, 16-byte aligned:
+//   whole-row tiles (rows ya .. ya + rn - 1): per plane i the rows ya - c_y .. as one copy, two
+//     where they wrap past row ny - 1, into plane i's stage rows at pitch stride; the mask rows
+//     ya - 1 .. ya + rn, one copy each;
+//   strip tiles: per row segment g (row y, strips j_lo .. j_hi of the row), the 9 plane rows
+//     y - c_y over the segment's cells plus a 16-byte halo each side (clipped to the row), the
+//     mask rows y - 1, y, y + 1 from the aligned word below the segment's first cell, and where
+//     the segment starts at x = 0 (ends at x = nx - 1) the 16-byte blocks holding column nx - 1
+//     of planes 1, 5, 8 (column 0 of planes 3, 6, 7).
+// Every copy is checked against its source buffer and its stage region before upload; a plan
+// that would leave them is an internal error, reported instead of launched.
+template <class ST, int kW, int kC>
+int build_plan(lbm_batch* b) {
+  using S = FlatShape<ST, kW, kC>;
+  constexpr long long es = static_cast<long long>(sizeof(ST));
+  std::vector<TilePlan> plans;
+  std::vector<CopyOp> ops;
+  plans.reserve(static_cast<size_t>(b->tiles));
+  const long long state_bytes = b->total_elems * es, mask_bytes = b->mask_words_total * 4;
+  bool ok = true;
+  // One copy: source byte offset (state or mask buffer), stage byte offset, bytes.
+  auto add = [&](long long src, bool from_mask, long long dst, long long bytes, long long dst_lo,
+                 long long dst_hi) {
+    if (bytes <= 0) return 0LL;
+    ok = ok && src % 16 == 0 && dst % 16 == 0 && bytes % 16 == 0 && src >= 0 && dst >= dst_lo &&
+         dst + bytes <= dst_hi && src + bytes <= (from_mask ? mask_bytes : state_bytes) &&
+         src / 16 <= 0xffffffffLL && dst / 16 < 0x10000 && bytes / 16 < kCopyFromMask;
+    if (ok)
+      ops.push_back(CopyOp{static_cast<uint32_t>(src / 16), static_cast<uint16_t>(dst / 16),
+                           static_cast<uint16_t>(bytes / 16 | (from_mask ? kCopyFromMask : 0))});
+    return bytes;
+  };
+  for (int k = 0; k < b->count && ok; ++k) {
+    const auto& in = b->inst[k];
+    const Grid2D& g = in.g;
+    const int nx = g.nx, ny = g.ny, pitch = g.pitch;
+    const int spr = (nx + S::SW - 1) / S::SW;
+    const int rpt = spr <= kW ? kW / spr : 0;
+    const int ntiles = rpt ? (ny + rpt - 1) / rpt
+                           : static_cast<int>((static_cast<long long>(spr) * ny + kW - 1) / kW);
+    for (int j = 0; j < ntiles; ++j) {
+      TilePlan h{};
+      h.first = static_cast<int>(ops.size());
+      long long bytes = 0;
+      if (rpt) {
+        const int ya = j * rpt, rn = std::min(rpt, ny - ya);
+        h.inst_nseg = k;
+        h.ya = ya;
+        h.a = rn;
+        for (int i = 0; i < kQ; ++i) {
+          int r0 = ya - dir_cy(i);
+          r0 = r0 < 0 ? r0 + ny : (r0 >= ny ? r0 - ny : r0);
+          const int len0 = std::min(rn, ny - r0);
+          const long long plane0 = in.off + i * g.plane;
+          const long long lo = i * S::SROW * es, hi = (i + 1) * S::SROW * es;
+          bytes += add((plane0 + static_cast<long long>(r0) * pitch) * es, false, lo, len0 * pitch * es, lo, hi);
+          bytes += add(plane0 * es, false, lo + len0 * pitch * es, (rn - len0) * pitch * es, lo, hi);
+        }
+        for (int r = 0; r < rn + 2; ++r) {
+          int m = ya - 1 + r;
+          m = m < 0 ? m + ny : (m >= ny ? m - ny : m);
+          bytes += add((in.mask_off + static_cast<long long>(m) * g.mask_words) * 4, true,
+                       S::kPlaneBytes + r * S::MW * 4, S::MW * 4, S::kPlaneBytes,
+                       S::kPlaneBytes + S::kMaskBytes);
+        }
+      } else {
+        const int s0 = j * kW, s1 = std::min(s0 + kW, spr * ny);
+        const int ya = s0 / spr, nseg = (s1 - 1) / spr - ya + 1;
+        h.inst_nseg = k | (nseg << 16);
+        h.ya = ya;
+        h.a = s0;
+        h.b = s1;
+        for (int sgi = 0; sgi < nseg; ++sgi) {
+          const Segment sg = tile_segment(sgi, s0, s1, ya, spr);
+          const int y = sg.y, ym = y == 0 ? ny - 1 : y - 1, yp = y == ny - 1 ? 0 : y + 1;
+          const int x0 = sg.j_lo * S::SW;
+          const int xs = std::max(x0 - S::H, 0);
+          const int xe = std::min((sg.j_hi + 1) * S::SW + S::H, pitch);
+          for (int q = 0; q < kQ; ++q) {
+            const long long lo = q * S::SROW * es, hi = (q + 1) * S::SROW * es;
+            const long long dst = (q * S::SROW + sg.w_first * S::SW + 2 * sgi * S::H + (xs - (x0 - S::H))) * es;
+            bytes += add((in.off + q * g.plane + static_cast<long long>(plan_src_row(q, y, ym, yp)) * pitch + xs) * es,
+                         false, dst, (xe - xs) * es, lo, hi);
+          }
+          const int rows3[3] = {ym, y, yp};
+          for (int r = 0; r < 3; ++r)
+            bytes += add((in.mask_off + static_cast<long long>(rows3[r]) * g.mask_words + (((sg.j_lo * S::SW) >> 5) & ~3)) * 4,
+                         true, S::kPlaneBytes + (sgi * 3 + r) * S::MW * 4, S::MW * 4, S::kPlaneBytes,
+                         S::kPlaneBytes + S::kMaskBytes);
+          for (int wj = 0; wj < 6; ++wj) {
+            const bool lo_end = wj < 3;
+            if (lo_end ? sg.j_lo != 0 : sg.j_hi != spr - 1) continue;
+            const int i = plan_wrap_dir(wj);
+            const int xb = lo_end ? ((nx - 1) & ~(S::H - 1)) : 0;
+            const long long wlo = S::kPlaneBytes + S::kMaskBytes;
+            bytes += add((in.off + i * g.plane + static_cast<long long>(plan_src_row(i, y, ym, yp)) * pitch + xb) * es,
+                         false, wlo + (sgi * 6 + wj) * S::H * es, 16, wlo, wlo + S::kWrapBytes);
+          }
+        }
+      }
+      h.ncopy = static_cast<int>(ops.size()) - h.first;
+      h.bytes = static_cast<int>(bytes);
+      plans.push_back(h);
+    }
+  }
+  if (!ok || static_cast<long long>(plans.size()) != b->tiles)
+    return bfail(b, LBM_ERR_CUDA, "internal error: a ring tile's copy plan leaves its buffers");
+  if (ops.empty()) ops.push_back(CopyOp{0, 0, 0});
+  if (b->plans_cap < static_cast<long long>(plans.size())) {
+    cudaFree(b->plans_d);
+    b->plans_d = nullptr;
+    b->plans_cap = 0;
+    B_CUDA(b, cudaMalloc(&b->plans_d, plans.size() * sizeof(TilePlan)));
+    b->plans_cap = static_cast<long long>(plans.size());
+  }
+  if (b->ops_cap < static_cast<long long>(ops.size())) {
+    cudaFree(b->ops_d);
+    b->ops_d = nullptr;
+    b->ops_cap = 0;
+    B_CUDA(b, cudaMalloc(&b->ops_d, ops.size() * sizeof(CopyOp)));
+    b->ops_cap = static_cast<long long>(ops.size());
+  }
+  B_CUDA(b, cudaMemcpy(b->plans_d, plans.data(), plans.size() * sizeof(TilePlan), cudaMemcpyHostToDevice));
+  B_CUDA(b, cudaMemcpy(b->ops_d, ops.data(), ops.size() * sizeof(CopyOp), cudaMemcpyHostToDevice));
+  b->plan_sw = S::SW;
+  b->plan_kw = kW;
+  b->plan_kc = kC;
   return LBM_OK;
 }
 
@@ -680,6 +701,8 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
       b->table_kw = kW;
       if (int rc = build_table<ST>(b, b->table_G ? b->table_G : StoreTraits<ST>::kVec)) return rc;
     }
+    if (b->plan_sw != S::SW || b->plan_kw != kW || b->plan_kc != kC)
+      if (int rc = build_plan<ST, kW, kC>(b)) return rc;
     B_CUDA(b, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
     int grid = b->grid;
     if (grid <= 0) {
@@ -699,7 +722,8 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
   a.step = b->step_d;
   a.args = static_cast<const StagedArgs<ST, Phys>*>(b->args_d);
   a.tiles = b->tiles;
-  a.heads = static_cast<const TileHead*>(b->heads_d);
+  a.plans = static_cast<const TilePlan*>(b->plans_d);
+  a.ops = static_cast<const CopyOp*>(b->ops_d);
   int* err = reinterpret_cast<int*>(b->step_d + 1);
   for (int s = 0; s < steps; ++s) {
     a.src = static_cast<const ST*>(b->buf[b->cur]);
@@ -1023,6 +1047,7 @@ int lbm_batch_create(int count, const int* nx, const int* ny, const uint8_t* con
     b->total_cells += static_cast<long long>(nx[k]) * ny[k];
   }
   b->total_elems = off;
+  b->mask_words_total = moff;
   if (cudaGetDevice(&b->device) != cudaSuccess ||
       cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device) != cudaSuccess ||
       cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking) != cudaSuccess ||
@@ -1050,7 +1075,7 @@ int lbm_batch_destroy(lbm_batch* b) {
   if (!b) return LBM_OK;
   if (b->stream) cudaStreamSynchronize(b->stream);
   drop_graph(b);
-  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->args_d, b->heads_d, b->stage,
+  for (void* p : {b->buf[0], b->buf[1], static_cast<void*>(b->mask_d), b->table_d, b->args_d, b->plans_d, b->ops_d, b->stage,
                   static_cast<void*>(b->red), static_cast<void*>(b->step_d)})
     cudaFree(p);
   for (cudaEvent_t ev : b->ev)

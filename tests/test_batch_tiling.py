@@ -1,5 +1,6 @@
 """CPU model of the batched ensemble's ring tiling (<pkg>/csrc/batch.cu: build_table's tile
-rule, BatchFlatPolicy::issue / copy / row_copy and the strip descriptors the consumers use).
+rule, build_plan's copies of each tile and the strip descriptors BatchFlatPolicy::issue writes
+for the consumers).
 
 The index arithmetic is restated here line by line and checked for every tile shape the
 library accepts (consumer warps x passes: 8x2, 4x2, 4x1, 2x2), every storage width (FP32,
