@@ -710,7 +710,7 @@ def run_ours(args):
         if args.adjoint:
             forms["adjoint"] = adjoint_report(pkg, peak)
         if args.batch:
-            forms["batch"] = batch_report(pkg, peak, args.batch_autotune)
+            forms["batch"] = batch_report(pkg, peak, args.batch_autotune, args.batch_steps)
         if args.scale:
             forms["scale"] = scale_report(pkg, peak)
         if args.wake:
@@ -859,6 +859,8 @@ def main():
                     help="skip the batched ensemble form")
     ap.add_argument("--no-batch-autotune", dest="batch_autotune", action="store_false",
                     help="batched ensemble with the library's default launch (profiling)")
+    ap.add_argument("--batch-steps", type=int, default=5000,
+                    help="timed steps of the batched ensemble (the workload's 5000; fewer for profiling)")
     ap.add_argument("--no-scale", dest="scale", action="store_false",
                     help="skip the 2048^2 / 4096^2 / 8192^2 FP32 and FP64 scale report")
     ap.add_argument("--no-wake", dest="wake", action="store_false",
