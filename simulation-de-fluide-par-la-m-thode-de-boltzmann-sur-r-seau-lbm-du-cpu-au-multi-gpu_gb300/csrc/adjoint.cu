@@ -184,6 +184,17 @@ __device__ __forceinline__ uint32_t field_bytes(const AdjGeom& g, int tx0, int e
   return static_cast<uint32_t>((xe - tx0) * elem);
 }
 
+template <class S>
+__device__ __forceinline__ void issue_mask_rows(unsigned char* dst, const uint32_t* mask, const AdjGeom& g,
+                                                const TilePos& t, uint64_t* full) {
+  uint32_t* sm = reinterpret_cast<uint32_t*>(dst);
+  const int r3[3] = {t.ym, t.y, t.yp};
+#pragma unroll
+  for (int r = 0; r < 3; ++r)
+    bulk_copy_g2s(sm + r * S::MW, mask + static_cast<size_t>(r3[r]) * g.mask_words + (t.tx0 >> 5), S::MW * 4,
+                  full);
+}
+
 // Warp vote: does any cell of warp cw's strip (32 kC cells), or a neighbour of one, lie in a
 // solid? Mask words w0 .. w0 + kC of the 3 staged rows, w0 = cw kC.
 template <class S>
@@ -237,34 +248,33 @@ __device__ __forceinline__ void staged_pull(const T* st, const T* wr, int nx, in
   }
 }
 
-// Producer copies shared by both sweeps, one per lane of the producer warp: lane i < 9 the pull
-// row of plane i of state R, lanes 12-14 the wrap blocks of column nx - 1 (where the tile starts
-// at x = 0), lanes 15-17 those of column 0 (where it ends at x = nx - 1).
+// Producer copies shared by both sweeps: the 9 pull rows of state R and their wrap blocks.
 template <class T, class S>
-__device__ __forceinline__ void issue_pull_lane(unsigned char* st, unsigned char* wrap, const T* R, const AdjGeom& g,
-                                                const TilePos& t, const RowSpan<S>& rs, bool lo, bool hi,
-                                                uint64_t* full, int lane) {
-  if (lane < kQ) {
-    bulk_copy_g2s(reinterpret_cast<T*>(st) + lane * S::SROW + rs.dst0,
-                  R + lane * g.plane + static_cast<long long>(src_row(lane, t.y, t.ym, t.yp)) * g.pitch + rs.xs,
-                  rs.bytes, full);
-  } else if (lane >= 12 && lane < 18) {
-    const int j = lane - 12;
-    if (j < 3 ? !lo : !hi) return;
-    const int i = wrap_dir(j);
-    const int xb = j < 3 ? ((g.nx - 1) & ~(S::H - 1)) : 0;
-    bulk_copy_g2s(reinterpret_cast<T*>(wrap) + j * S::H,
-                  R + i * g.plane + static_cast<long long>(src_row(i, t.y, t.ym, t.yp)) * g.pitch + xb, 16, full);
+__device__ __forceinline__ void issue_pull(unsigned char* st, unsigned char* wrap, const T* R, const AdjGeom& g,
+                                           const TilePos& t, const RowSpan<S>& rs, bool lo, bool hi,
+                                           uint64_t* full) {
+  T* rows = reinterpret_cast<T*>(st);
+#pragma unroll
+  for (int i = 0; i < kQ; ++i)
+    bulk_copy_g2s(rows + i * S::SROW + rs.dst0,
+                  R + i * g.plane + static_cast<long long>(src_row(i, t.y, t.ym, t.yp)) * g.pitch + rs.xs, rs.bytes,
+                  full);
+  T* wr = reinterpret_cast<T*>(wrap);
+  if (lo) {
+    const int xb = (g.nx - 1) & ~(S::H - 1);
+    for (int j = 0; j < 3; ++j) {
+      const int i = wrap_dir(j);
+      bulk_copy_g2s(wr + j * S::H, R + i * g.plane + static_cast<long long>(src_row(i, t.y, t.ym, t.yp)) * g.pitch + xb,
+                    16, full);
+    }
   }
-}
-
-// Mask row r (0: y - 1, 1: y, 2: y + 1) of a tile.
-template <class S>
-__device__ __forceinline__ void issue_mask_row(unsigned char* dst, const uint32_t* mask, const AdjGeom& g,
-                                               const TilePos& t, uint64_t* full, int r) {
-  const int row = r == 0 ? t.ym : (r == 1 ? t.y : t.yp);
-  bulk_copy_g2s(reinterpret_cast<uint32_t*>(dst) + r * S::MW,
-                mask + static_cast<size_t>(row) * g.mask_words + (t.tx0 >> 5), S::MW * 4, full);
+  if (hi) {
+    for (int j = 3; j < 6; ++j) {
+      const int i = wrap_dir(j);
+      bulk_copy_g2s(wr + j * S::H, R + i * g.plane + static_cast<long long>(src_row(i, t.y, t.ym, t.yp)) * g.pitch,
+                    16, full);
+    }
+  }
 }
 
 // Warp sum (fixed shuffle tree) of one value per lane, added by lane 0 to *slot.
@@ -289,26 +299,20 @@ struct AdjForward {
   using S = AdjRing<T, kC>;
   using L = FwdStage<T, kC>;
   static constexpr bool kFinish = true;
-  static constexpr bool kWarpIssue = true;
   const FwdArgs<T>& p;
   int cur_b = -1;  // instance of the lane sums
   T usum = T(0);   // this lane's sum of u_x over the instance's cells it collided
 
-  // The producer warp's lanes issue the tile's copies in parallel, one each (lane 0 arms the
-  // barrier first): lanes 0-8 the pull rows, 9-11 the mask rows, 12-17 the wrap blocks, 18 the
-  // alpha row. One lane issuing them in turn was what limited the sweep.
-  __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
+  __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full) const {
     const AdjGeom& g = p.g;
     const TilePos t = tile_pos<S::TW>(g, p.at, tile, p.reverse);
     const RowSpan<S> rs(g, t.tx0, sizeof(T));
     const bool lo = t.tx0 == 0, hi = t.tx0 + S::TW >= g.nx;
     const uint32_t fb = p.alpha ? field_bytes<S>(g, t.tx0, sizeof(T)) : 0u;
-    if (lane == 0)
-      mbar_arrive_expect_tx(full, kQ * rs.bytes + S::kMaskBytes + (lo ? 48u : 0u) + (hi ? 48u : 0u) + fb);
-    __syncwarp();
-    issue_pull_lane<T, S>(base, base + L::kWrap, p.R + t.b * g.inst, g, t, rs, lo, hi, full, lane);
-    if (lane >= kQ && lane < kQ + 3) issue_mask_row<S>(base + L::kMask, p.mask, g, t, full, lane - kQ);
-    if (lane == 18 && fb)
+    mbar_arrive_expect_tx(full, kQ * rs.bytes + S::kMaskBytes + (lo ? 48u : 0u) + (hi ? 48u : 0u) + fb);
+    issue_pull<T, S>(base, base + L::kWrap, p.R + t.b * g.inst, g, t, rs, lo, hi, full);
+    issue_mask_rows<S>(base + L::kMask, p.mask, g, t, full);
+    if (fb)
       bulk_copy_g2s(base + L::kAlpha, p.alpha + t.b * g.plane + static_cast<long long>(t.y) * g.pitch + t.tx0, fb,
                     full);
   }
@@ -478,16 +482,11 @@ struct AdjBackward {
   using S = AdjRing<T, kC>;
   using L = BwdStage<T, kC>;
   static constexpr bool kFinish = true;
-  static constexpr bool kWarpIssue = true;
   const BwdArgs<T>& p;
   int cur_b = -1;
   T go = T(0), gx = T(0), gy = T(0);
 
-  // The producer warp's lanes issue the tile's copies in parallel (lane 0 arms the barrier
-  // first): copy c = lane, lane + 32 of: 0-8 the pull rows of R, 9-11 the mask rows, 12-17 the
-  // wrap blocks of R, 18-26 the transpose rows of Z, 27-32 the wrap blocks of Z, 33 the alpha
-  // row, 34 the alpha_bar segment row.
-  __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full, int lane) const {
+  __device__ __forceinline__ void issue(int tile, unsigned char* base, uint64_t* full) const {
     const AdjGeom& g = p.g;
     const TilePos t = tile_pos<S::TW>(g, p.at, tile, p.reverse);
     const RowSpan<S> rs(g, t.tx0, sizeof(T));
@@ -496,38 +495,39 @@ struct AdjBackward {
     const uint32_t fa = p.alpha ? field_bytes<S>(g, t.tx0, sizeof(T)) : 0u;
     const uint32_t fs = p.aseg ? field_bytes<S>(g, t.tx0, sizeof(T)) : 0u;
     const uint32_t wraps = (lo ? 48u : 0u) + (hi ? 48u : 0u);
-    if (lane == 0)
-      mbar_arrive_expect_tx(full, (z ? 2u : 1u) * (kQ * rs.bytes + wraps) + S::kMaskBytes + fa + fs);
-    __syncwarp();
-    const long long f0 = t.b * g.plane + static_cast<long long>(t.y) * g.pitch + t.tx0;
-    for (int c = lane; c < 35; c += 32) {
-      if (c < 18) {
-        issue_pull_lane<T, S>(base, base + L::kWrapR, p.R + t.b * g.inst, g, t, rs, lo, hi, full, c);
-        if (c >= kQ && c < kQ + 3) issue_mask_row<S>(base + L::kMask, p.mask, g, t, full, c - kQ);
-      } else if (c < 27) {
-        if (!z) continue;
-        const int j = c - 18;
-        bulk_copy_g2s(reinterpret_cast<T*>(base + L::kZ) + j * S::SROW + rs.dst0,
-                      p.Z + t.b * g.inst + j * g.plane + static_cast<long long>(tr_row(j, t.y, t.ym, t.yp)) * g.pitch +
-                          rs.xs,
+    mbar_arrive_expect_tx(full, (z ? 2u : 1u) * (kQ * rs.bytes + wraps) + S::kMaskBytes + fa + fs);
+    issue_pull<T, S>(base, base + L::kWrapR, p.R + t.b * g.inst, g, t, rs, lo, hi, full);
+    issue_mask_rows<S>(base + L::kMask, p.mask, g, t, full);
+    if (z) {
+      const T* Z = p.Z + t.b * g.inst;
+      T* rows = reinterpret_cast<T*>(base + L::kZ);
+#pragma unroll
+      for (int j = 0; j < kQ; ++j)
+        bulk_copy_g2s(rows + j * S::SROW + rs.dst0,
+                      Z + j * g.plane + static_cast<long long>(tr_row(j, t.y, t.ym, t.yp)) * g.pitch + rs.xs,
                       rs.bytes, full);
-      } else if (c < 33) {
-        // Wrap blocks of the transpose: planes 1, 5, 8 (c_x = +1) at x = nx - 1 read column 0;
-        // planes 3, 6, 7 (c_x = -1) at x = 0 read column nx - 1.
-        const int j = c - 27;
-        if (!z || (j < 3 ? !hi : !lo)) continue;
-        const int i = wrap_dir(j);
-        const int xb = j < 3 ? 0 : ((g.nx - 1) & ~(S::H - 1));
-        bulk_copy_g2s(reinterpret_cast<T*>(base + L::kWrapZ) + j * S::H,
-                      p.Z + t.b * g.inst + i * g.plane + static_cast<long long>(tr_row(i, t.y, t.ym, t.yp)) * g.pitch +
-                          xb,
-                      16, full);
-      } else if (c == 33) {
-        if (fa) bulk_copy_g2s(base + L::kAlpha, p.alpha + f0, fa, full);
-      } else {
-        if (fs) bulk_copy_g2s(base + L::kAseg, p.aseg + f0, fs, full);
+      // Wrap blocks of the transpose: planes 1, 5, 8 (c_x = +1) at x = nx - 1 read column 0;
+      // planes 3, 6, 7 (c_x = -1) at x = 0 read column nx - 1.
+      T* wz = reinterpret_cast<T*>(base + L::kWrapZ);
+      if (hi) {
+        for (int j = 0; j < 3; ++j) {
+          const int i = wrap_dir(j);
+          bulk_copy_g2s(wz + j * S::H, Z + i * g.plane + static_cast<long long>(tr_row(i, t.y, t.ym, t.yp)) * g.pitch,
+                        16, full);
+        }
+      }
+      if (lo) {
+        const int xb = (g.nx - 1) & ~(S::H - 1);
+        for (int j = 3; j < 6; ++j) {
+          const int i = wrap_dir(j);
+          bulk_copy_g2s(wz + j * S::H,
+                        Z + i * g.plane + static_cast<long long>(tr_row(i, t.y, t.ym, t.yp)) * g.pitch + xb, 16, full);
+        }
       }
     }
+    const long long f0 = t.b * g.plane + static_cast<long long>(t.y) * g.pitch + t.tx0;
+    if (fa) bulk_copy_g2s(base + L::kAlpha, p.alpha + f0, fa, full);
+    if (fs) bulk_copy_g2s(base + L::kAseg, p.aseg + f0, fs, full);
   }
 
   __device__ __forceinline__ void flush(int cw, int lane) {
