@@ -557,14 +557,14 @@ def adjoint_report(pkg, peak):
     nx, ny, tau, fx, steps, window, batch = 512, 128, 0.6, 5e-6, 2000, 100, 32
     mask = pkg.workloads.adjoint_channel(nx, ny)
     fields = pkg.workloads.brinkman_batch(nx, ny, batch, mask, seed=1234)
-    out = {}
+    out, grads = {}, {}
     for prec in ("fp32", "fp64"):
         try:
             with pkg.Adjoint(nx, ny, tau, fx, 0.0, mask, precision=prec, batch=batch,
                              checkpoint_every=100) as a:
                 a.set_alpha(fields)
                 a.forward(steps, window)
-                a.backward()
+                grads[prec] = a.backward()
                 f, b = a.step_times()
             cells = nx * ny * batch
             out[prec] = {"forward_step_us": round(f * 1e6, 2), "backward_step_us": round(b * 1e6, 2),
@@ -573,6 +573,14 @@ def adjoint_report(pkg, peak):
                          "backward_mlups": round(cells / b / 1e6, 1)}
         except Exception as e:
             out[prec] = {"error": str(e)[:200]}
+    if len(grads) == 2:  # the FP32 adjoint against the FP64 one, over the 32 instances
+        g32, g64 = grads["fp32"], grads["fp64"]
+        rel = lambda a, b: float(np.max(np.abs(np.asarray(a) - np.asarray(b)) / np.abs(np.asarray(b))))
+        a32, a64 = np.asarray(g32["alpha"]), np.asarray(g64["alpha"])
+        big = np.abs(a64) > 1e-3 * np.max(np.abs(a64))
+        out["fp32_vs_fp64_max_rel"] = {"fx": float(f"{rel(g32['fx'], g64['fx']):.3g}"),
+                                       "tau": float(f"{rel(g32['tau'], g64['tau']):.3g}"),
+                                       "alpha": float(f"{float(np.max(np.abs(a32 - a64)[big] / np.abs(a64)[big])):.3g}")}
     out["workload"] = (f"channel {nx}x{ny}, tau {tau}, F=({fx},0), {batch} distinct seeded "
                        f"Brinkman alpha fields in [0,0.1], {steps} steps, J window {window}, K=100")
     return out
