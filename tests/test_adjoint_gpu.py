@@ -96,8 +96,10 @@ def test_fp32_adjoint_matches_fp64(setup, adjoint64):
         J32 = a.forward(STEPS, WINDOW)[0]
         g32 = a.backward()
     assert J32 == pytest.approx(J64, rel=1e-4)
-    assert g32["fx"][0] == pytest.approx(g64["fx"][0], rel=1e-3)
-    assert g32["tau"][0] == pytest.approx(g64["tau"][0], rel=1e-3)
+    # the parameter gradients to the finite-difference bar (measured on the 32-field batch:
+    # 3e-6 for F_x, 3e-5 for tau); per-cell alpha gradients to 1e-3 on the seeded cells
+    assert g32["fx"][0] == pytest.approx(g64["fx"][0], rel=1e-4)
+    assert g32["tau"][0] == pytest.approx(g64["tau"][0], rel=1e-4)
     a32, a64 = g32["alpha"][0][cells], g64["alpha"][0][cells]
     assert np.max(np.abs(a32 - a64) / np.abs(a64)) < 1e-3
 
