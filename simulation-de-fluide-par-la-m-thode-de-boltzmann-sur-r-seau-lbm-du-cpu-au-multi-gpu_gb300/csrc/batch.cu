@@ -970,8 +970,9 @@ int time_steps(lbm_batch* b, int steps, double* seconds) {
 
 // Revision of the batch kernels in autotuner cache keys: raised whenever a change can reorder
 // the candidates or change what a cached launch means (2: two producer warps per ring block and
-// the resident-block caps that come with them), so that older cached choices are timed again.
-constexpr int kBatchKernelRev = 2;
+// the resident-block caps that come with them; 3: the host-built copy plan), so that older
+// cached choices are timed again.
+constexpr int kBatchKernelRev = 3;
 
 std::string tune_key(const lbm_batch* b) {
   cudaDeviceProp prop{};
