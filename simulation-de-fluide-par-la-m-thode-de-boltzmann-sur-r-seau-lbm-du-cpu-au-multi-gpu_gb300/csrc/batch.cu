@@ -23,6 +23,7 @@
 #include <new>
 #include <sstream>
 #include <string>
+#include <type_traits>
 #include <vector>
 
 #include "aux_kernels.cuh"
@@ -314,11 +315,23 @@ struct BatchFlatPolicy {
   __device__ __forceinline__ void consume(int, const unsigned char* base, int cw, int lane) const {
     const StripDesc sd = reinterpret_cast<const StripDesc*>(base + kDescOff)[cw];
     if (!(sd.flags & kStripValid)) return;
-    const StepArgs<ST, Phys>& p = reinterpret_cast<const StagedArgs<ST, Phys>*>(base + S::kStageBytes)->p;
-    if (sd.flags & kStripRows)
-      strip<true>(p, sd, base, lane);
-    else
-      strip<false>(p, sd, base, lane);
+    const StagedArgs<ST, Phys>* sa = reinterpret_cast<const StagedArgs<ST, Phys>*>(base + S::kStageBytes);
+    if constexpr (std::is_same_v<ST, float>) {
+      // FP32: the step arguments as a local copy, which lets the compiler keep the fields the
+      // collision uses in registers across the strip instead of reading them from the stage at
+      // every use (+1.8 % on the benchmark ensemble; the 16-bit collision has no registers to
+      // spare and lost 10 % with it).
+      const StepArgs<ST, Phys> p = sa->p;
+      if (sd.flags & kStripRows)
+        strip<true>(p, sd, base, lane);
+      else
+        strip<false>(p, sd, base, lane);
+    } else {
+      if (sd.flags & kStripRows)
+        strip<true>(sa->p, sd, base, lane);
+      else
+        strip<false>(sa->p, sd, base, lane);
+    }
   }
 
   __device__ __forceinline__ void finish(int, int) const {}
@@ -331,11 +344,13 @@ __host__ __device__ constexpr size_t batch_ring_smem(int stages) {
 }
 
 // Resident blocks per SM the register budget of a ring shape is capped for (blocks of kW
-// consumer and two producer warps): 30 to 32 warps per SM at 64 registers for the FP32
-// collision, 20 to 28 warps at 73 to 80 registers for the 16-bit one (which spills under 72),
-// none for FP64 (FP64-ALU-bound: its kernels are compiled without a register cap).
+// consumer and two producer warps): 24 to 32 warps per SM for the FP32 collision (4 blocks of
+// the 4x2 shape, which its 4-stage ring's shared memory allows anyway, leave it the registers
+// to hold the step arguments), 20 to 28 warps at 73 to 80 registers for the 16-bit one (which
+// spills under 72), none for FP64 (FP64-ALU-bound: its kernels are compiled without a register
+// cap).
 __host__ __device__ constexpr int batch_ring_blocks(int elem, int kW) {
-  return elem == 8 ? 1 : elem == 2 ? (kW == 8 ? 2 : (kW == 4 ? 4 : 7)) : (kW == 8 ? 3 : (kW == 4 ? 5 : 8));
+  return elem == 8 ? 1 : elem == 2 ? (kW == 8 ? 2 : (kW == 4 ? 4 : 7)) : (kW == 8 ? 3 : (kW == 4 ? 4 : 8));
 }
 // Most resident blocks per SM the autotuner tries for a ring shape: the register cap above,
 // and for FP64 what its uncapped registers let reside (blocks of kW consumer warps and one

@@ -28,7 +28,7 @@ DEFAULTS = [
     ("solver.cu", "ring_step_kernel<float, ExactPhys<ExactF32>, 0, 8, 2, 2, 1>", 9, 3),
     ("solver.cu", "ring_step_kernel<__half, FastPhys, 0, 8, 4, 2, 2>", 9, 2),
     ("solver.cu", "ring_step_kernel<__nv_bfloat16, FastPhys, 0, 8, 4, 2, 2>", 9, 2),
-    ("batch.cu", "batch_ring_kernel<float, ExactPhys<ExactF32>, 4, 2, 4>", 6, 5),
+    ("batch.cu", "batch_ring_kernel<float, ExactPhys<ExactF32>, 4, 2, 4>", 6, 4),
     ("batch.cu", "batch_ring_kernel<__half, FastPhys, 4, 2, 4>", 6, 4),
     # FP64 ring shapes at the most blocks per SM the autotuner tries (batch_ring_tune_blocks)
     ("batch.cu", "batch_ring_kernel<double, ExactPhys<ExactF64>, 8, 2, 2>", 9, 2),
