@@ -763,7 +763,9 @@ struct lbm_adjoint {
   const void* fin = nullptr;     // R_T after the forward (a state buffer or a checkpoint slot)
   bool have_forward = false;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;  // the second half of the batch (forward sweep)
   cudaEvent_t ev[2] = {nullptr, nullptr};
+  cudaEvent_t join = nullptr;      // orders the two halves' streams
   double fwd_step_s = 0, bwd_step_s = 0;
   int sm_count = 0;
   std::string err;
@@ -904,31 +906,62 @@ FwdArgs<typename A::T> fwd_args(const lbm_adjoint* a) {
 }
 
 template <class K, class Args>
-int launch_ring(lbm_adjoint* a, K kernel, int grid, size_t smem, const Args& p) {
-  ADJ_CUDA(a, launch_dependent(kernel, dim3(grid), dim3(kAdjThreads), smem, a->stream, p, a->err_d));
+int launch_ring(lbm_adjoint* a, K kernel, int grid, size_t smem, const Args& p, cudaStream_t stream) {
+  ADJ_CUDA(a, launch_dependent(kernel, dim3(grid), dim3(kAdjThreads), smem, stream, p, a->err_d));
   return LBM_OK;
 }
 
+// One half of the batch for the forward sweep: its instances' arguments and where they start in
+// the batch's state, field and slot arrays. The two halves run on two streams, so that one
+// half's launch fills the SMs while the other's drains (a sweep step is a short kernel, and
+// its fill and drain cost a sixth of it when one launch holds the whole batch).
+template <class T>
+struct FwdHalf {
+  FwdArgs<T> p;
+  long long state_off = 0, slot_off = 0;
+  cudaStream_t stream = nullptr;
+};
+
 template <class A>
-int launch_forward(lbm_adjoint* a, FwdArgs<typename A::T> p, const void* R, void* Rn, double* obj, int reverse) {
+FwdHalf<typename A::T> fwd_half(const lbm_adjoint* a, const FwdArgs<typename A::T>& p, int k);
+
+template <class A>
+int launch_forward(lbm_adjoint* a, const FwdHalf<typename A::T>& h, const void* R, void* Rn, double* obj,
+                   int reverse) {
   using T = typename A::T;
-  p.R = static_cast<const T*>(R);
-  p.Rn = static_cast<T*>(Rn);
-  p.obj = obj;
+  FwdArgs<T> p = h.p;
+  p.R = static_cast<const T*>(R) + h.state_off;
+  p.Rn = Rn ? static_cast<T*>(Rn) + h.state_off : nullptr;
+  p.obj = obj ? obj + h.slot_off : nullptr;
   p.reverse = reverse;
   return with_shape<T>(a->fwd_c, [&](auto kc) {
     constexpr int kC = decltype(kc)::value;
-    return launch_ring(a, AdjKernels<A, kC>::fwd, a->fwd_grid, AdjLaunch<T, kC>::fwd_smem(), p);
+    return launch_ring(a, AdjKernels<A, kC>::fwd, a->fwd_grid, AdjLaunch<T, kC>::fwd_smem(), p, h.stream);
   });
 }
 
 template <class A>
-int launch_backward(lbm_adjoint* a, const BwdArgs<typename A::T>& p) {
+int launch_backward(lbm_adjoint* a, const BwdArgs<typename A::T>& p, cudaStream_t stream) {
   using T = typename A::T;
   return with_shape<T>(a->bwd_c, [&](auto kc) {
     constexpr int kC = decltype(kc)::value;
-    return launch_ring(a, AdjKernels<A, kC>::bwd, a->bwd_grid, AdjLaunch<T, kC>::bwd_smem(), p);
+    return launch_ring(a, AdjKernels<A, kC>::bwd, a->bwd_grid, AdjLaunch<T, kC>::bwd_smem(), p, stream);
   });
+}
+
+// Number of halves the batch runs as (two when it has at least two instances) and the first
+// instance of half k.
+inline int adj_halves(const lbm_adjoint* a) { return a->batch >= 2 ? 2 : 1; }
+inline int adj_half_first(const lbm_adjoint* a, int k) { return k == 0 ? 0 : a->batch / 2; }
+inline int adj_half_count(const lbm_adjoint* a, int k) {
+  return adj_halves(a) == 1 ? a->batch : (k == 0 ? a->batch / 2 : a->batch - a->batch / 2);
+}
+
+// Makes stream `to` wait for the work enqueued so far on stream `from`.
+inline cudaError_t adj_join(lbm_adjoint* a, cudaStream_t from, cudaStream_t to) {
+  cudaError_t e = cudaEventRecord(a->join, from);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(to, a->join, 0);
+  return e;
 }
 
 // Per-instance sums of nval-valued slots into host memory (synchronises the stream), then the
@@ -946,6 +979,21 @@ int read_sums(lbm_adjoint* a, const double* slots, int grid, int nval, std::vect
     return adj_fail(a, LBM_ERR_TIMEOUT, "an adjoint kernel gave up waiting for its shared-memory ring");
   }
   return LBM_OK;
+}
+
+// Half k of the batch for the forward sweep (the whole batch when it runs undivided).
+template <class A>
+FwdHalf<typename A::T> fwd_half(const lbm_adjoint* a, const FwdArgs<typename A::T>& p, int k) {
+  FwdHalf<typename A::T> h;
+  const long long b0 = adj_half_first(a, k);
+  h.p = p;
+  h.p.g.batch = adj_half_count(a, k);
+  h.p.at = make_tiles(h.p.g, a->fwd_c, a->fwd_grid);
+  h.state_off = b0 * a->g.inst;
+  h.slot_off = b0 * a->fwd_grid * kAdjW;
+  if (p.alpha) h.p.alpha = p.alpha + b0 * a->g.plane;
+  h.stream = k == 0 ? a->stream : a->stream2;
+  return h;
 }
 
 template <class A>
@@ -979,20 +1027,31 @@ int forward_t(lbm_adjoint* a, const void* s0_host, int steps, int window, double
     ADJ_CUDA(a, cudaMemsetAsync(ckpt, 0, sb, a->stream));  // rest: f_i - w_i = 0
   }
   ADJ_CUDA(a, cudaMemsetAsync(a->obj_part, 0, a->obj_slots * sizeof(double), a->stream));
+  // The batch as two halves on two streams (one launch per half and step), or whole.
   const FwdArgs<T> p = fwd_args<A>(a);
+  const int nhalf = adj_halves(a);
+  FwdHalf<T> half[2];
+  for (int k = 0; k < nhalf; ++k) half[k] = fwd_half<A>(a, p, k);
   const void* cur = ckpt;
   int spare = 0;
   ADJ_CUDA(a, cudaEventRecord(a->ev[0], a->stream));
+  if (nhalf == 2) ADJ_CUDA(a, adj_join(a, a->stream, a->stream2));
   for (int t = 0; t < steps; ++t) {
     const bool in_window = t >= steps - window + 1;
     const bool is_ckpt = (t + 1) % a->K == 0;
     void* out = is_ckpt ? ckpt + static_cast<size_t>((t + 1) / a->K) * sb : a->state[spare];
-    if (const int rc = launch_forward<A>(a, p, cur, out, in_window ? a->obj_part : nullptr, t & 1)) return rc;
+    for (int k = 0; k < nhalf; ++k)
+      if (const int rc = launch_forward<A>(a, half[k], cur, out, in_window ? a->obj_part : nullptr, t & 1)) return rc;
     if (!is_ckpt) spare ^= 1;
     cur = out;
   }
+  if (nhalf == 2) ADJ_CUDA(a, adj_join(a, a->stream2, a->stream));
   ADJ_CUDA(a, cudaEventRecord(a->ev[1], a->stream));
-  if (const int rc = launch_forward<A>(a, p, cur, nullptr, a->obj_part, steps & 1)) return rc;  // final state's objective
+  // the final state's objective
+  if (nhalf == 2) ADJ_CUDA(a, adj_join(a, a->stream, a->stream2));
+  for (int k = 0; k < nhalf; ++k)
+    if (const int rc = launch_forward<A>(a, half[k], cur, nullptr, a->obj_part, steps & 1)) return rc;
+  if (nhalf == 2) ADJ_CUDA(a, adj_join(a, a->stream2, a->stream));
   ADJ_CUDA(a, cudaGetLastError());
   std::vector<double> sums;
   if (const int rc = read_sums(a, a->obj_part, a->fwd_grid, 1, sums)) return rc;
@@ -1045,9 +1104,29 @@ int backward_t(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* d
   pb.grads = a->grad_part;
   const T coef = T(1.0 / (static_cast<double>(W) * a->fluid));
   char* seg = static_cast<char*>(a->seg);
+  // The batch as two halves on two streams, as in the forward sweep: per half its instances'
+  // recomputation and adjoint arguments, offset into the batch's arrays.
+  const int nhalf = adj_halves(a);
+  FwdHalf<T> fh[2];
+  BwdArgs<T> bh[2];
+  long long st_off[2] = {0, 0};
+  cudaStream_t hs[2] = {a->stream, a->stream2};
+  for (int k = 0; k < nhalf; ++k) {
+    fh[k] = fwd_half<A>(a, pf, k);
+    const long long b0 = adj_half_first(a, k);
+    st_off[k] = b0 * a->g.inst;
+    bh[k] = pb;
+    bh[k].g.batch = adj_half_count(a, k);
+    bh[k].at = make_tiles(bh[k].g, a->bwd_c, a->bwd_grid);
+    if (pb.alpha) bh[k].alpha = pb.alpha + b0 * a->g.plane;
+    if (pb.aseg) bh[k].aseg = pb.aseg + b0 * a->g.plane;
+    bh[k].abar = pb.abar + b0 * a->g.plane;
+    bh[k].grads = pb.grads + 3 * b0 * a->bwd_grid * kAdjW;
+  }
   int yb = 0;
   bool first = true;
   ADJ_CUDA(a, cudaEventRecord(a->ev[0], a->stream));
+  if (nhalf == 2) ADJ_CUDA(a, adj_join(a, a->stream, a->stream2));
   const int nseg = (T_steps + K - 1) / K;
   for (int s = nseg - 1; s >= 0; --s) {
     const int t0 = s * K, t1 = std::min(T_steps, t0 + K);
@@ -1055,23 +1134,28 @@ int backward_t(lbm_adjoint* a, double* dtau, double* dfx, double* dfy, double* d
     const char* base = static_cast<const char*>(a->ckpt) + static_cast<size_t>(s) * sb;
     auto state_at = [&](int t) -> const void* { return t == t0 ? base : seg + static_cast<size_t>(t - t0 - 1) * sb; };
     for (int t = t0; t < t1; ++t)
-      if (const int rc = launch_forward<A>(a, pf, state_at(t), seg + static_cast<size_t>(t - t0) * sb, nullptr, t & 1))
-        return rc;
+      for (int k = 0; k < nhalf; ++k)
+        if (const int rc = launch_forward<A>(a, fh[k], state_at(t), seg + static_cast<size_t>(t - t0) * sb, nullptr, t & 1))
+          return rc;
     // Adjoint steps t1 (only for the last segment: the final state) .. t0.
     const int top = (s == nseg - 1) ? t1 : t1 - 1;
     for (int t = top; t >= t0; --t) {
       const bool in_window = t >= T_steps - W + 1;
-      pb.R = static_cast<const T*>(state_at(t));
-      pb.Z = first ? nullptr : static_cast<const T*>(a->ybar[yb ^ 1]);
-      pb.Yb = static_cast<T*>(a->ybar[yb]);
-      pb.obj_coef = in_window ? coef : T(0);
-      pb.flush = t == t0 ? 1 : 0;
-      pb.reverse = t & 1;
-      if (const int rc = launch_backward<A>(a, pb)) return rc;
+      for (int k = 0; k < nhalf; ++k) {
+        BwdArgs<T>& q = bh[k];
+        q.R = static_cast<const T*>(state_at(t)) + st_off[k];
+        q.Z = first ? nullptr : static_cast<const T*>(a->ybar[yb ^ 1]) + st_off[k];
+        q.Yb = static_cast<T*>(a->ybar[yb]) + st_off[k];
+        q.obj_coef = in_window ? coef : T(0);
+        q.flush = t == t0 ? 1 : 0;
+        q.reverse = t & 1;
+        if (const int rc = launch_backward<A>(a, q, hs[k])) return rc;
+      }
       first = false;
       yb ^= 1;
     }
   }
+  if (nhalf == 2) ADJ_CUDA(a, adj_join(a, a->stream2, a->stream));
   ADJ_CUDA(a, cudaEventRecord(a->ev[1], a->stream));
   ADJ_CUDA(a, cudaGetLastError());
   if (dalpha)
@@ -1150,6 +1234,8 @@ int lbm_adj_create(int nx, int ny, const uint8_t* solid, double tau, double fx, 
   if (cudaGetDevice(&dev) != cudaSuccess ||
       cudaDeviceGetAttribute(&a->sm_count, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
       cudaStreamCreateWithFlags(&a->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&a->stream2, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&a->join, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreate(&a->ev[0]) != cudaSuccess || cudaEventCreate(&a->ev[1]) != cudaSuccess)
     return fail(LBM_ERR_CUDA);
   if (const int rc = precision == LBM_FP64 ? configure<ExactF64>(a) : configure<ExactF32>(a)) return fail(rc);
@@ -1181,7 +1267,9 @@ int lbm_adj_destroy(lbm_adjoint* a) {
     cudaFree(p);
   for (cudaEvent_t ev : a->ev)
     if (ev) cudaEventDestroy(ev);
+  if (a->join) cudaEventDestroy(a->join);
   if (a->stream) cudaStreamDestroy(a->stream);
+  if (a->stream2) cudaStreamDestroy(a->stream2);
   delete a;
   return LBM_OK;
 }
