@@ -495,7 +495,9 @@ def wake_report(pkg):
     (momentum exchange on the device, sampled every 50 steps), lift rms and mean drag over the
     second half; against the FP64 run: the velocity L2 error of the mean flow (u averaged over
     the second half, sampled every 500 steps: the shedding phase drifts between forms, so the
-    instantaneous fields decorrelate) and of the final field, and each run's mass drift."""
+    instantaneous fields decorrelate) and of the final field, and each run's mass drift.
+    The 16-bit forms also report St over four noise streams (step-counter offsets 0, 7, 1001,
+    50000): the wake has two shedding states and their rounding noise picks one per stream."""
     out, runs = {}, {}
     for prec in ("fp64", "fp32", "fp16", "bf16"):
         try:
@@ -517,6 +519,18 @@ def wake_report(pkg):
                 out[prec]["st_rel_diff_vs_fp64"] = round(out[prec]["st"] / out["fp64"]["st"] - 1.0, 5)
                 out[prec]["velocity_l2_mean_flow"] = float(f"{pkg.wake.velocity_l2(got, ref, 'mean'):.4g}")
                 out[prec]["velocity_l2_final"] = float(f"{pkg.wake.velocity_l2(got, ref, 'end'):.4g}")
+    for prec in ("fp16", "bf16"):
+        if "st" not in out.get(prec, {}):
+            continue
+        try:
+            sts = [out[prec]["st"]] + [round(pkg.wake.strouhal(pkg.wake.lift_series(
+                pkg, prec, steps=200_000, every=50, noise_offset=off))["st"], 5) for off in (7, 1001, 50000)]
+            st32 = out.get("fp32", {}).get("st")
+            out[prec]["streams"] = {"offsets": [0, 7, 1001, 50000], "st": sts,
+                                    "within_2pct_of_fp32": (sum(1 for x in sts if abs(x / st32 - 1) < 0.02)
+                                                            if st32 else None)}
+        except Exception as e:
+            out[prec]["streams"] = {"error": str(e)[:200]}
     out["workload"] = ("cylinder wake 1024x256, disc D=32 at (256,129), tau 0.548, Re 100, "
                        f"F=({pkg.wake.WAKE_FORCE:.4g},0) calibrated for u_bulk 0.05, 200k steps, "
                        "lift sampled every 50 steps")

@@ -178,11 +178,11 @@ __device__ __forceinline__ float2 widen_pair<__nv_bfloat16>(uint32_t raw) {
 
 // One pair of cells x, x + 1 (x even) of a strip, 16-bit storage, FP32 fast collision. Same
 // stage layout (and kWrapInRow, kHalo) as ring_cell; word / lane locate the pair's mask bits
-// (cells x - 1 .. x + 2).
+// (cells x - 1 .. x + 2); rkey is the step's stochastic-rounding key (step_rkey).
 template <class ST, bool kOpen, class S, bool kWrapInRow = false, bool kHalo = false>
 __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const ST* st,
                                           const uint32_t* sm, const ST* wr, int y, int x, int lx,
-                                          int word, int lane, bool solids) {
+                                          int word, int lane, bool solids, uint32_t rkey) {
   const int nx = p.g.nx;
   const long long plane = p.g.plane;
   const long long row = static_cast<long long>(y) * p.g.pitch;
@@ -274,7 +274,7 @@ __device__ __forceinline__ void ring_pair(const StepArgs<ST, FastPhys>& p, const
   }
   float2 out[kQ];
   collide_fast_t<FastF32x2>(v, p.k, out);
-  const uint32_t ph = sr_pair_hash(p.key_base + row + x, step_rkey(p));
+  const uint32_t ph = sr_pair_hash(p.key_base + row + x, rkey);
   uint32_t* d = reinterpret_cast<uint32_t*>(p.dst + row + x);
   uint32_t w[kQ];
 #pragma unroll
@@ -367,7 +367,8 @@ __device__ __forceinline__ void ring_consume_tile(const StepArgs<ST, Phys>& p, c
     const int x = xw + 32 * S::LC * c + S::LC * lane;
     if (x < nx) {
       if constexpr (S::LC == 2)
-        ring_pair<ST, kOpen, S, false, kHalo>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids);
+        ring_pair<ST, kOpen, S, false, kHalo>(p, st, sm, wr, y, x, x - tx0 + S::H, w0 + 2 * c, lane, solids,
+                                              step_rkey(p));
       else
         ring_cell<ST, typename Phys::Arith, kOpen, S, false, kHalo>(p, st, sm, wr, y, ym, yp, x, x - tx0 + S::H, w0 + c,
                                                      lane, solids);

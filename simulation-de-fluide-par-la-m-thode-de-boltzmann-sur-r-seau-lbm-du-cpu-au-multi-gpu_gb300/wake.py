@@ -69,12 +69,15 @@ WAKE_FORCE = 6.784303312490499e-07
 
 def lift_series(pkg, precision: str, steps: int = 200_000, every: int = 50, variant: int = -1,
                 nx: int = NX, ny: int = NY, d: float = D, tau: float = TAU, u0: float = U0,
-                force: float | None = None, mean_every: int = 0):
+                force: float | None = None, mean_every: int = 0, noise_offset: int = 0):
     """Runs the wake and samples the force on the disc every `every` steps. Returns a dict of
     numpy arrays t, drag, lift, the bulk velocity u_bulk, the final velocity field (ux_end,
     uy_end, float64) and the total mass at the start and the end (mass0, mass1). With
     mean_every > 0 (a multiple of `every`), also the velocity field averaged over the second
-    half of the run, sampled every mean_every steps (ux_mean, uy_mean)."""
+    half of the run, sampled every mean_every steps (ux_mean, uy_mean). noise_offset > 0
+    advances the step counter, which keys the stochastic rounding of the 16-bit forms, by that
+    many steps before the same start state: another noise stream of the same run (no effect on
+    the deterministic FP32 / FP64 forms)."""
     solid, disc = geometry(nx, ny, d)
     fx = force if force is not None else (WAKE_FORCE or wake_force(tau, u0, ny - 2))
     n = steps // every
@@ -86,6 +89,9 @@ def lift_series(pkg, precision: str, steps: int = 200_000, every: int = 50, vari
         if variant >= 0:
             s.set_variant(variant)
         s.init_equilibrium(1.0, u0, 0.0)
+        if noise_offset:
+            s.run(noise_offset)
+            s.init_equilibrium(1.0, u0, 0.0)
         s.set_body(disc)
         mass0 = s.total_mass()
         for k in range(n):
