@@ -232,7 +232,7 @@ struct BatchFlatPolicy {
   // The step's stochastic-rounding key (16-bit storage), read from the step counter once per
   // launch instead of once per strip pass (a global load on the consumers' path: +3 % on the
   // 256-channel benchmark ensemble in FP16). The single-grid ring keeps the load per pass, which
-  // there measured 2 % faster than one per tile.
+  // there measured 2 to 3 % faster than one per tile or one per launch.
   uint32_t rkey;
 
   // Producer (all 32 lanes): the lanes describe the consumer warps' strips, lane 0 copies the
