@@ -8,8 +8,8 @@
 //     strips one more (at least 2 rows each); its buffers hold local rows 0 .. n_k + 1, row 0 and
 //     row n_k + 1 being the ghost copies of global rows y0 - 1 and y0 + n_k (periodic ring);
 //   * one step = one launch of the ring step kernel over the owned rows of every strip (rows
-//     1 .. n_k, whose y-neighbours are all local; a tile finds its strip by binary search over
-//     the strips' first tiles), with the halo exchange fused into it: the ghost row below
+//     1 .. n_k, whose y-neighbours are all local; a tile finds its strip from its row by the
+//     decomposition's arithmetic), with the halo exchange fused into it: the ghost row below
 //     strip k receives the populations moving up (c_y = +1: 2, 5, 6) of the top owned row of the
 //     strip below, the ghost row above receives those moving down (c_y = -1: 4, 7, 8) of the
 //     bottom owned row of the strip above: 3 * nx values per message, the reference's halo
@@ -31,6 +31,7 @@
 #include <vector>
 
 #include "aux_kernels.cuh"
+#include "fastdiv.h"
 #include "forms.cuh"
 #include "lbm_b200.h"
 #include "solver_internal.h"
@@ -64,25 +65,42 @@ struct StripTile {
 };
 constexpr int kStripTableSmem = 256;  // strip tables up to this size are staged in shared memory
 
+// How the owned rows split into strips (the reference's make_strip): the first `extra` strips own
+// base + 1 rows, the others base; a global owned row's strip and local row follow from two
+// divisions by invariant divisors.
+struct StripSplit {
+  int base, extra;
+  FastDiv by_long, by_short;  // by base + 1, by base
+  __device__ __forceinline__ void locate(int row, int& k, int& local) const {
+    const int split = extra * (base + 1);
+    if (row < split) {
+      k = static_cast<int>(by_long.div(static_cast<uint32_t>(row)));
+      local = row - k * (base + 1);
+    } else {
+      const int q = static_cast<int>(by_short.div(static_cast<uint32_t>(row - split)));
+      k = extra + q;
+      local = row - split - q * base;
+    }
+  }
+};
+
 // Tiles of all strips for the ring pipeline: tpr tiles per row, the owned rows of strip 0, then
-// of strip 1, ...; the grid of a tile is the strip's (base arguments with the strip's offsets).
+// of strip 1, ... (the lattice's rows in order); the grid of a tile is the strip's (base
+// arguments with the strip's offsets).
 template <class ST, class Phys, int kTW>
 struct StripTiles {
   const StepArgs<ST, Phys>& base;  // src / dst / mask: buffer bases; g: nx, pitch, mask words
   const StripTile* tab;
-  int strips, tpr, tiles, reverse;  // reverse: walk the tiles from the last (alternate steps)
+  const StripSplit& split;
+  FastDiv tpr;
+  int tiles, reverse;  // reverse: walk the tiles from the last (alternate steps)
   template <class F>
   __device__ __forceinline__ void visit(int tile, F&& f) const {
     if (reverse) tile = tiles - 1 - tile;
-    int lo = 0, hi = strips - 1;
-    while (lo < hi) {
-      const int mid = (lo + hi + 1) >> 1;
-      if (tab[mid].tile0 <= tile)
-        lo = mid;
-      else
-        hi = mid - 1;
-    }
-    const StripTile& t = tab[lo];
+    const int row = static_cast<int>(tpr.div(static_cast<uint32_t>(tile)));
+    int k, r;
+    split.locate(row, k, r);
+    const StripTile& t = tab[k];
     StepArgs<ST, Phys> p = base;
     p.src = base.src + t.off;
     p.dst = base.dst + t.off;
@@ -91,9 +109,7 @@ struct StripTiles {
     p.g.plane = t.plane;
     p.key_base = t.key_base;
     p.halo = t.halo;
-    const int local = tile - t.tile0;
-    const int r = local / tpr;
-    f(p, r + 1, (local - r * tpr) * kTW);
+    f(p, r + 1, (tile - row * static_cast<int>(tpr.d)) * kTW);
   }
 };
 
@@ -102,8 +118,8 @@ struct StripTiles {
 // bottom owned rows (the ghost rows of the destination buffer are complete when it ends).
 template <class ST, class Phys, bool kOpen, int kC, int kMinBlocks>
 __global__ void __launch_bounds__(32 * 9, kMinBlocks)
-    strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips, int tpr,
-                      int tiles, int reverse, int* err) {
+    strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips,
+                      const StripSplit split, FastDiv tpr, int tiles, int reverse, int* err) {
   using S = RingShape<ST, 8, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
@@ -115,7 +131,7 @@ __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     t = s_tab;
   }
   using Tiles = StripTiles<ST, Phys, S::TW>;
-  const Tiles tiles_of{base, t, strips, tpr, tiles, reverse};
+  const Tiles tiles_of{base, t, split, tpr, tiles, reverse};
   ring_pipeline<ST, Phys, kOpen, 8, kC, 2, Tiles, true>(smem, tiles_of, tiles, err);
 }
 
@@ -261,12 +277,18 @@ int steps_tc(lbm_strips* h, int steps) {
   a.sc = h->sc;
   a.step_ctr = h->ctr;
   int* err = reinterpret_cast<int*>(h->ctr + 1);
+  StripSplit split{};
+  split.base = h->ny / h->strips;
+  split.extra = h->ny % h->strips;
+  split.by_long = FastDiv(static_cast<uint32_t>(split.base + 1));
+  split.by_short = FastDiv(static_cast<uint32_t>(split.base));
   for (int s = 0; s < steps; ++s) {
     a.src = static_cast<const ST*>(h->buf[h->cur]);
     a.dst = static_cast<ST*>(h->buf[h->cur ^ 1]);
     a.step_off = static_cast<uint32_t>(s);
     S_CUDA(h, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, h->stream, a,
-                               static_cast<const StripTile*>(h->tiles_d), h->strips, tpr, tiles, h->cur, err));
+                               static_cast<const StripTile*>(h->tiles_d), h->strips, split,
+                               FastDiv(static_cast<uint32_t>(tpr)), tiles, h->cur, err));
     h->cur ^= 1;
   }
   counter_add_kernel<<<1, 1, 0, h->stream>>>(h->ctr, static_cast<uint32_t>(steps));
