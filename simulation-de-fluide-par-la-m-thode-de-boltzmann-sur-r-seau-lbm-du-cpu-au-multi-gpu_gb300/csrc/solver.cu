@@ -222,8 +222,8 @@ int launch_ring_t(lbm_solver* s, int steps) {
       a.step_off = static_cast<uint32_t>(k);
       // Odd steps (by buffer parity) walk the tiles backwards: they start on the rows the
       // previous step wrote last.
-      LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, s->stream, a,
-                                   FastDiv(static_cast<uint32_t>(tpr)), tiles, 0, s->cur, s->err_flag));
+      LBM_CUDA(s, launch_dependent(kernel, dim3(grid), dim3(S::kThreads), smem, s->stream, a, tpr, tiles, 0,
+                                   s->cur, s->err_flag));
       s->cur ^= 1;
     }
     LBM_CUDA(s, cudaGetLastError());

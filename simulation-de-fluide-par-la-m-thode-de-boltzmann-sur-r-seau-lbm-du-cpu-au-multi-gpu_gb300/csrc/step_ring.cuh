@@ -28,7 +28,6 @@
 #include <type_traits>
 #include <utility>
 
-#include "fastdiv.h"
 #include "step_tma.cuh"
 
 namespace lbm_b200 {
@@ -539,24 +538,23 @@ __device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& 
 // blocks walk them from the last one, so that a step started right after one that walked
 // forward first reads the rows that step wrote last, which are still in L2 (the launches
 // alternate: on a 4096^2 FP32 grid the 129 MB L2 holds about a sixth of a 604 MB state).
-// The producer and every consumer warp decode each tile, so the row comes from a division by
-// an invariant divisor (FastDiv) rather than the integer division's instruction sequence.
+// (A multiply-high division by the invariant tiles_per_row, as the strip engine decodes its
+// tiles, made the FP32 step 3 % slower here: 88.3k against 91.0k MLUPS at 4096^2.)
 template <class ST, class Phys, int kTW>
 struct GridTiles {
   const StepArgs<ST, Phys>& p;
-  FastDiv tiles_per_row;
-  int row0, tiles, reverse;
+  int tiles_per_row, row0, tiles, reverse;
   template <class F>
   __device__ __forceinline__ void visit(int tile, F&& f) const {
     if (reverse) tile = tiles - 1 - tile;
-    const int tr = static_cast<int>(tiles_per_row.div(static_cast<uint32_t>(tile)));
-    f(p, row0 + tr, (tile - tr * static_cast<int>(tiles_per_row.d)) * kTW);
+    const int tr = tile / tiles_per_row;
+    f(p, row0 + tr, (tile - tr * tiles_per_row) * kTW);
   }
 };
 
 template <class ST, class Phys, bool kOpen, int kW, int kC, int kStages, int kMinBlocks>
 __global__ void __launch_bounds__(32 * (kW + 1), kMinBlocks)
-    ring_step_kernel(const StepArgs<ST, Phys> p, FastDiv tiles_per_row, int tiles, int row0, int reverse, int* err) {
+    ring_step_kernel(const StepArgs<ST, Phys> p, int tiles_per_row, int tiles, int row0, int reverse, int* err) {
   using S = RingShape<ST, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
