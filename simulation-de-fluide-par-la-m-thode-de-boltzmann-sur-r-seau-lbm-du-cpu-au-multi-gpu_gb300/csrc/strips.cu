@@ -55,13 +55,13 @@ struct StripView {
 };
 
 // A strip as the step kernel sees it: offsets of its planes and mask rows, its rounding-key
-// base (cell offset of global row y0 - 1), owned rows and first tile of the step's tile index,
+// base (cell offset of global row y0 - 1), owned rows,
 // and the fused halo's targets (StepArgs::halo): ghost row 0 of the strip above and ghost row
 // n + 1 of the strip below, as offsets from this strip's planes, with their plane strides.
 struct StripTile {
   long long off, plane, key_base, moff;
   long long halo[4];
-  int n, tile0;
+  int n;
 };
 constexpr int kStripTableSmem = 256;  // strip tables up to this size are staged in shared memory
 
@@ -553,14 +553,12 @@ int lbm_strips_create(int nx, int ny, const uint8_t* solid, double tau, double f
     e = cudaMemcpy(h->mask_d, all_words.data(), all_words.size() * sizeof(uint32_t), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMalloc(&h->views_d, strips * sizeof(StripView));
   if (e == cudaSuccess) e = cudaMemcpy(h->views_d, views.data(), strips * sizeof(StripView), cudaMemcpyHostToDevice);
-  // The step kernel's strip table: tiles of the ring shape (8 consumer warps x 2 passes: 512
-  // cells per tile, 1024 with 16-bit storage) over the owned rows, strip after strip.
+  // The step kernel's strip table (its tiles: the ring shape of 8 consumer warps x 2 passes, 512
+  // cells per tile, 1024 with 16-bit storage, or 4 passes for 16-bit storage on rows of at
+  // least 2048 cells, over the owned rows, strip after strip).
   {
     h->passes = (elem == 2 && nx >= 2048) ? 4 : 2;
-    const int tw = 32 * 8 * h->passes * (elem == 2 ? 2 : 1);
-    const int tpr = (nx + tw - 1) / tw;
     std::vector<StripTile> tt(strips);
-    int tile0 = 0;
     for (int k = 0; k < strips; ++k) {
       const int up = k == strips - 1 ? 0 : k + 1, dn = k == 0 ? strips - 1 : k - 1;
       StripTile& t = tt[k];
@@ -573,8 +571,6 @@ int lbm_strips_create(int nx, int ny, const uint8_t* solid, double tau, double f
       t.halo[2] = h->off[dn] + static_cast<long long>(h->n[dn] + 1) * h->pitch - h->off[k];  // row n + 1 below
       t.halo[3] = views[dn].plane;
       t.n = h->n[k];
-      t.tile0 = tile0;
-      tile0 += tpr * h->n[k];
     }
     if (e == cudaSuccess) e = cudaMalloc(&h->tiles_d, strips * sizeof(StripTile));
     if (e == cudaSuccess) e = cudaMemcpy(h->tiles_d, tt.data(), strips * sizeof(StripTile), cudaMemcpyHostToDevice);
