@@ -236,7 +236,11 @@ int launch_ring_t(lbm_solver* s, int steps) {
 // 51.7k (v12 47.4k / 46.2k), 1024^2 v17 83.9k (v12 81.7k), 2048^2 v12 86.2k, 4096^2 v12 90.6k;
 // 16-bit storage: 256^2 v19 20.2k (v0 13.5k), 512^2 v19 61.2k, 1024^2 v19 114.5k (v17 108.6k,
 // v20 91.1k: its 2048-cell tiles are half empty on 1024-cell rows), 2048^2 v20 157.1k (v17
-// 143.0k), 4096^2 v20 168.7k (v17 159.3k). Rows narrower than 256 cells take the
+// 143.0k), 4096^2 v20 168.7k (v17 159.3k). With the one-instruction stochastic conversion
+// (fewer instructions per cell) the 16-bit sweep moved on the largest grids (walled channel,
+// seeded state, best of 3): 2048^2 v20 170.6k (v17 149.7k), 4096^2 v20 169.5k (v17 169.0k,
+// v22 170.3k), 8192^2 v17 175.7k (v20 168.9k), so grids of at least 2^25 cells take v17.
+// Rows narrower than 256 cells take the
 // direct kernel (0), whose 128-cell chunks leave fewer lanes idle than the rings' wide tiles
 // (FP64 on 100 x 2000: the ring 12 reached 1.0k MLUPS with a fifth of its lanes busy); otherwise
 // FP64 (FP64-ALU-bound) takes the ring 12 with at least two of its tiles per SM, else 0.
@@ -251,6 +255,7 @@ int auto_variant(const lbm_solver* s) {
   }
   if (sizeof(ST) == 2) {
     if (cells < (2LL << 20)) return 19;
+    if (cells >= (32LL << 20)) return 17;
     return (s->nx >= 2048 && cells >= (4LL << 20)) ? 20 : 17;  // 2048-cell tiles need wide rows
   }
   return cells < (1LL << 17) ? 19 : (cells < (2LL << 20) ? 17 : 12);
