@@ -183,7 +183,7 @@ int lbm_set_launch(lbm_solver* s, int block_threads, int grid_blocks);
  * serialisation (the next step's blocks are scheduled while the previous step drains).
  * -1 (the default), by grid size from a sweep on GB300: rows narrower than 256 cells: 0; plain
  * FP32: 19 below 2^17 cells, 17 below 2^21, 12 above; 16-bit storage: 19 below 2^21 cells, 20
- * with rows of at least 2048 cells and at least 2^22 cells, 17 otherwise; FP64: 12 with at least
+ * with rows of at least 2048 cells and 2^22 to 2^25 cells, 17 otherwise; FP64: 12 with at least
  * two 512-cell tiles per SM, 0 otherwise.
  * The 16-bit forms round stored populations stochastically (see lbm_create); every variant
  * derives the same random bits, so the variants give the same results. */
