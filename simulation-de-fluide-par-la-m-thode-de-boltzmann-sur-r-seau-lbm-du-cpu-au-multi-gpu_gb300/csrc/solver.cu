@@ -295,7 +295,8 @@ template <class ST>
 int launch_steps(lbm_solver* s, int steps) {
   const int rc = s->open_x ? launch_steps_o<ST, true>(s, steps) : launch_steps_o<ST, false>(s, steps);
   if (rc) return rc;
-  counter_add_kernel<<<1, 1, 0, s->stream>>>(s->step_ctr, static_cast<uint32_t>(steps));
+  LBM_CUDA(s, launch_dependent(counter_add_dep_kernel, dim3(1), dim3(1), 0, s->stream, s->step_ctr,
+                               static_cast<uint32_t>(steps)));
   LBM_CUDA(s, cudaGetLastError());
   return LBM_OK;
 }
