@@ -84,22 +84,24 @@ struct StripSplit {
   }
 };
 
-// Tiles of all strips for the ring pipeline: tpr tiles per row, the owned rows of strip 0, then
-// of strip 1, ... (the lattice's rows in order); the grid of a tile is the strip's (base
-// arguments with the strip's offsets).
-template <class ST, class Phys, int kTW>
-struct StripTiles {
+// Stage policy of the strips' tiles for the ring pipeline: tpr tiles per row, the owned rows of
+// strip 0, then of strip 1, ... (the lattice's rows in order); the grid of a tile is the strip's
+// (base arguments with the strip's offsets). The producer decodes each tile once and hands its
+// strip, local row and first cell to the consumer warps in 16 bytes after the ring stage
+// (written before it arms the stage, read after the wait), so that eight consumer warps do not
+// repeat the divisions.
+template <class ST, class Phys, bool kOpen, int kC>
+struct StripPolicy {
+  using S = RingShape<ST, 8, kC>;
+  static constexpr bool kFinish = false;
+  static constexpr int kStageBytes = S::kStageBytes + 16;
   const StepArgs<ST, Phys>& base;  // src / dst / mask: buffer bases; g: nx, pitch, mask words
   const StripTile* tab;
   const StripSplit& split;
   FastDiv tpr;
   int tiles, reverse;  // reverse: walk the tiles from the last (alternate steps)
-  template <class F>
-  __device__ __forceinline__ void visit(int tile, F&& f) const {
-    if (reverse) tile = tiles - 1 - tile;
-    const int row = static_cast<int>(tpr.div(static_cast<uint32_t>(tile)));
-    int k, r;
-    split.locate(row, k, r);
+
+  __device__ __forceinline__ StepArgs<ST, Phys> strip_args(int k) const {
     const StripTile& t = tab[k];
     StepArgs<ST, Phys> p = base;
     p.src = base.src + t.off;
@@ -109,9 +111,33 @@ struct StripTiles {
     p.g.plane = t.plane;
     p.key_base = t.key_base;
     p.halo = t.halo;
-    f(p, r + 1, (tile - row * static_cast<int>(tpr.d)) * kTW);
+    return p;
   }
+
+  __device__ __forceinline__ void issue(int tile, unsigned char* stage, uint64_t* full) const {
+    if (reverse) tile = tiles - 1 - tile;
+    const int row = static_cast<int>(tpr.div(static_cast<uint32_t>(tile)));
+    int k, r;
+    split.locate(row, k, r);
+    const int tx0 = (tile - row * static_cast<int>(tpr.d)) * S::TW;
+    *reinterpret_cast<int4*>(stage + S::kStageBytes) = make_int4(k, r + 1, tx0, 0);
+    ring_issue_tile<ST, Phys, kOpen, S>(strip_args(k), stage, full, r + 1, tx0);
+  }
+
+  __device__ __forceinline__ void consume(int, const unsigned char* stage, int cw, int lane) const {
+    const int4 d = *reinterpret_cast<const int4*>(stage + S::kStageBytes);
+    ring_consume_tile<ST, Phys, kOpen, S, kC, true>(strip_args(d.x), stage, d.y, d.z, cw, lane);
+  }
+
+  __device__ __forceinline__ void finish(int, int) const {}
 };
+
+// Shared memory of a strip ring block: 2 stages of the policy, their barriers, then the strip
+// table when it is staged.
+template <class ST, class Phys, int kC>
+__host__ __device__ constexpr size_t strip_ring_smem() {
+  return 2 * static_cast<size_t>(StripPolicy<ST, Phys, false, kC>::kStageBytes) + 4 * sizeof(uint64_t);
+}
 
 // One step of every strip: the solver's ring kernel (8 consumer warps x kC passes, 2 stages)
 // over the strips' tiles, with the halo exchange fused into the stores of each strip's top and
@@ -120,19 +146,18 @@ template <class ST, class Phys, bool kOpen, int kC, int kMinBlocks>
 __global__ void __launch_bounds__(32 * 9, kMinBlocks)
     strip_ring_kernel(const StepArgs<ST, Phys> base, const StripTile* __restrict__ tab, int strips,
                       const StripSplit split, FastDiv tpr, int tiles, int reverse, int* err) {
-  using S = RingShape<ST, 8, kC>;
+  using Pol = StripPolicy<ST, Phys, kOpen, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
   grid_dependency_wait();
   const StripTile* t = tab;
   if (strips <= kStripTableSmem) {
-    StripTile* s_tab = reinterpret_cast<StripTile*>(smem + ring_smem_bytes<S>(2));
+    StripTile* s_tab = reinterpret_cast<StripTile*>(smem + strip_ring_smem<ST, Phys, kC>());
     for (int k = threadIdx.x; k < strips; k += blockDim.x) s_tab[k] = tab[k];
     __syncthreads();
     t = s_tab;
   }
-  using Tiles = StripTiles<ST, Phys, S::TW>;
-  const Tiles tiles_of{base, t, split, tpr, tiles, reverse};
-  ring_pipeline<ST, Phys, kOpen, 8, kC, 2, Tiles, true>(smem, tiles_of, tiles, err);
+  const Pol pol{base, t, split, tpr, tiles, reverse};
+  tile_pipeline<8, 2, Pol::kStageBytes>(smem, pol, tiles, err);
 }
 
 // Device halo exchange of all strips (raw elements E, the storage bits): thread per
@@ -260,7 +285,7 @@ int steps_tc(lbm_strips* h, int steps) {
   constexpr int kMin = sizeof(ST) == 8 ? 1 : ((kC == 4 && kOpen) ? 2 : 3);
   using S = RingShape<ST, 8, kC>;
   const auto kernel = strip_ring_kernel<ST, Phys, kOpen, kC, kMin>;
-  const size_t smem = ring_smem_bytes<S>(2) +
+  const size_t smem = strip_ring_smem<ST, Phys, kC>() +
                       (h->strips <= kStripTableSmem ? h->strips * sizeof(StripTile) : 0);
   S_CUDA(h, cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, static_cast<int>(smem)));
   int per_sm = 0;
