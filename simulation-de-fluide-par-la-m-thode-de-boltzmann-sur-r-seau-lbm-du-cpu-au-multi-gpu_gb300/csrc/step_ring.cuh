@@ -538,8 +538,10 @@ __device__ __forceinline__ void ring_pipeline(unsigned char* smem, const Tiles& 
 // blocks walk them from the last one, so that a step started right after one that walked
 // forward first reads the rows that step wrote last, which are still in L2 (the launches
 // alternate: on a 4096^2 FP32 grid the 129 MB L2 holds about a sixth of a 604 MB state).
-// (A multiply-high division by the invariant tiles_per_row, as the strip engine decodes its
-// tiles, made the FP32 step 3 % slower here: 88.3k against 91.0k MLUPS at 4096^2.)
+// Each consumer warp decodes the tile itself: a multiply-high division by the invariant
+// tiles_per_row made the FP32 step 3 % slower (88.3k against 91.0k MLUPS at 4096^2), and the
+// producer decoding once and handing the row to the consumers through the stage, as the strip
+// engine does with its heavier decoding, 1.4 % slower (89.4k against 90.7k).
 template <class ST, class Phys, int kTW>
 struct GridTiles {
   const StepArgs<ST, Phys>& p;
