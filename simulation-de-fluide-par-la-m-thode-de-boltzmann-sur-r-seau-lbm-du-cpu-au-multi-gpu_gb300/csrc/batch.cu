@@ -110,8 +110,12 @@ struct BatchArgs {
 };
 
 // Device step counter of a batch: read by every step launch, advanced by one after it (inside a
-// captured graph as well, so every replay of the graph rounds with fresh keys).
-__global__ void step_counter_add(uint32_t* c) { *c += 1u; }
+// captured graph as well, so every replay of the graph rounds with fresh keys). Behind a ring
+// step it is a dependent launch (it waits for the step to complete), as is the next step.
+__global__ void step_counter_add(uint32_t* c) {
+  grid_dependency_wait();
+  *c += 1u;
+}
 __global__ void step_counter_set(uint32_t* c, uint32_t v) { *c = v; }
 
 template <class ST, class Phys, int G>
@@ -374,6 +378,7 @@ __global__ void __launch_bounds__(FlatShape<ST, kW, kC>::kThreads, (batch_ring_m
     batch_ring_kernel(const BatchArgs<ST, Phys> a, int tiles, int* err) {
   using Pol = BatchFlatPolicy<ST, Phys, kW, kC>;
   extern __shared__ __align__(128) unsigned char smem[];
+  grid_dependency_wait();
   Pol pol{a, sizeof(ST) == 2 ? sr_step_key(__ldg(a.step)) : 0u};
   tile_pipeline<kW, kStages, Pol::kStageBytes, FlatShape<ST, kW, kC>::kProd>(smem, pol, tiles, err);
 }
@@ -749,8 +754,10 @@ int launch_batch_ring_t(lbm_batch* b, int steps, bool prepare_only) {
     a.src = static_cast<const ST*>(b->buf[b->cur]);
     a.dst = static_cast<ST*>(b->buf[b->cur ^ 1]);
     a.parity = b->cur;
-    kernel<<<b->grid_eff, S::kThreads, smem, b->stream>>>(a, b->tiles, err);
-    step_counter_add<<<1, 1, 0, b->stream>>>(b->step_d);
+    // Dependent launches (programmatic stream serialisation): the next launch is scheduled while
+    // this one drains (+0.1-0.2 % on the benchmark ensemble).
+    B_CUDA(b, launch_dependent(kernel, dim3(b->grid_eff), dim3(S::kThreads), smem, b->stream, a, b->tiles, err));
+    B_CUDA(b, launch_dependent(step_counter_add, dim3(1), dim3(1), 0, b->stream, b->step_d));
     ++b->t;
     b->cur ^= 1;
   }
