@@ -469,11 +469,13 @@ def accuracy_report(pkg):
 
 def scale_report(pkg, peak):
     """The plain method at every grid of the at-scale workload (walled channel, tau 0.6,
-    F = (1e-6, 0), seeded perturbation in [-1e-4, 1e-4]): 2048^2, 4096^2, 8192^2 in FP32
-    (1000 steps each) and FP64 (1000, 1000 and 200 steps: FP64-ALU-bound, 25 ms per step at
-    8192^2), device-resident MLUPS and the fraction of the 72 / 144 B per cell roofline."""
+    F = (1e-6, 0), seeded perturbation in [-1e-4, 1e-4]): 2048^2, 4096^2, 8192^2 in FP32 and
+    FP16 storage (1000 steps each) and FP64 (1000, 1000 and 200 steps: FP64-ALU-bound, 25 ms
+    per step at 8192^2), device-resident MLUPS and the fraction of the 72 / 36 / 144 B per cell
+    roofline."""
     out = {}
-    for prec, real, steps in (("fp32", "f32", (1000, 1000, 1000)), ("fp64", "f64", (1000, 1000, 200))):
+    for prec, real, steps in (("fp32", "f32", (1000, 1000, 1000)), ("fp16", "f32", (1000, 1000, 1000)),
+                              ("fp64", "f64", (1000, 1000, 200))):
         out[prec] = {}
         for n, k in zip((2048, 4096, 8192), steps):
             try:
